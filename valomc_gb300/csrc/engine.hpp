@@ -1,0 +1,85 @@
+// engine.hpp -- internal interface between the C ABI, the batch path and the serving loop.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "host_setup.hpp"
+
+namespace vmc {
+
+void set_error(const std::string &msg);
+int cuda_status(cudaError_t e, const char *what);
+#define VMC_CK(call)                                      \
+  do {                                                    \
+    cudaError_t _e = (call);                              \
+    if (_e != cudaSuccess) return cuda_status(_e, #call); \
+  } while (0)
+
+int select_device(int device, int *num_sms = nullptr);
+uint64_t clock_seed();
+
+// Resident geometry (the opaque vmc_mesh).
+struct DeviceMesh {
+  int device = 0;
+  int dim = 3;
+  HostMesh host;
+  void *d_geom[2] = {nullptr, nullptr};  // [precision]
+  double *d_bnorm = nullptr;
+  int64_t bytes = 0;
+  ~DeviceMesh();
+  const void *geom(int precision) const { return d_geom[precision]; }
+};
+int upload_mesh(DeviceMesh &m, int precision_mask);
+
+// Device state of one job.
+struct JobBuffers {
+  void *d_optics = nullptr;
+  uint8_t *d_bctype = nullptr;
+  double *d_bcn = nullptr, *d_cdf = nullptr;
+  SourceRec *d_src = nullptr;
+  double *d_acc = nullptr;  // ER, EI [Ne]; EBR, EBI, DEBR, DEBI [Nb]
+  unsigned long long *d_jc = nullptr;
+  double *d_ledger = nullptr;
+  uint32_t *d_tape = nullptr;
+  int64_t *d_tape_off = nullptr, *d_trace = nullptr, *d_trace_len = nullptr;
+  int64_t bytes = 0;
+  int64_t Ne = 0, Nb = 0;
+  ~JobBuffers();
+  void release();
+};
+// bytes of device state a job on mesh m needs (admission control)
+int64_t job_footprint(const HostJob &j, const HostMesh &m);
+int upload_job(const HostJob &j, const DeviceMesh &m, int precision, JobBuffers &b, cudaStream_t st);
+JobDev describe_job(const HostJob &j, const DeviceMesh &m, int precision, const JobBuffers &b);
+int zero_job(JobBuffers &b, cudaStream_t st);
+
+struct LaunchSpec {
+  int dim = 3, precision = VMC_FP32;
+  bool fd = false, tape = false;
+  int block = 0, blocks_per_sm = 0, chunk = 0;
+  int64_t max_steps = 0;
+};
+struct LaunchResult {
+  uint64_t steps = 0, scatters = 0, done = 0;
+  double kernel_ms = 0;
+  int grid = 0, block = 0;
+};
+// Runs the pool kernel over jobs (device descriptors are uploaded here) and waits,
+// polling progress / cancel / timeout from opt (may be null).  Stream-ordered.
+int launch_jobs(int device, const LaunchSpec &spec, const std::vector<JobDev> &jobs, const vmc_options *opt,
+                cudaStream_t st, LaunchResult &res);
+
+// Copies a job's accumulators and counters back and fills out/stats.
+int collect_job(const HostJob &j, const DeviceMesh &m, const JobBuffers &b, int64_t nphoton, bool normalize,
+                vmc_output *out, vmc_stats *st, cudaStream_t stream);
+
+const void *kernel_3d64(bool fd, bool tape);
+const void *kernel_3d32(bool fd, bool tape);
+const void *kernel_2d64(bool fd, bool tape);
+const void *kernel_2d32(bool fd, bool tape);
+const void *select_kernel(const LaunchSpec &s);
+
+}  // namespace vmc

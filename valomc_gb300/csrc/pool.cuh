@@ -1,0 +1,101 @@
+// pool.cuh -- the persistent photon-pool kernel.
+//
+// One CTA per SM slot stays resident for the whole run (the replacement of the reference's
+// OpenMP team, cpp/3d/MC3D.hpp:1670-1700).  Every lane carries one photon; when photons
+// end, the warp ballots its dead lanes and hands them the next indices from a warp-owned
+// chunk of the global photon counter (one atomic per chunk), so a warp never runs
+// half-empty while photons remain.  A photon index selects its job (batched launches),
+// its Philox stream (key = job seed, counter = photon index) or its tape segment, and the
+// walk advances one element step per loop iteration.  Each loop iteration polls nothing
+// but registers; the host cancel flag is read every 256 iterations.
+#pragma once
+#include "walk2d.cuh"
+
+namespace vmc {
+
+template <class R> __device__ __forceinline__ void start_rng(R &rng, const JobDev &J, int64_t q);
+template <> __device__ __forceinline__ void start_rng<PhiloxRng>(PhiloxRng &rng, const JobDev &J, int64_t q) {
+  rng.start(J.seed, J.stream, (uint64_t)(q + J.poffset));
+}
+template <> __device__ __forceinline__ void start_rng<TapeRng>(TapeRng &rng, const JobDev &J, int64_t q) {
+  rng.start_tape(J.tape + J.tape_off[q], J.tape + J.tape_off[q + 1]);
+}
+
+__device__ __forceinline__ int find_job(const LaunchParams &lp, int64_t p) {
+  int lo = 0, hi = lp.njobs - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (__ldg(lp.job_begin + mid) <= p) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+template <class W, class R>
+__global__ void __launch_bounds__(256) pool_kernel(const LaunchParams lp) {
+  W s;
+  R rng;
+  const JobDev *J = lp.jobs;
+  bool alive = false, done = false;
+  uint32_t n_steps = 0, n_scat = 0, n_done = 0;
+  long long chunk_next = 0, chunk_end = 0;
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  const long long total = lp.total;
+  for (unsigned it = 0;; ++it) {
+    if ((it & 255u) == 0u) {
+      if (*reinterpret_cast<volatile const int32_t *>(&lp.ctl->cancel)) { done = true; alive = false; }
+    }
+    unsigned need = __ballot_sync(kFull, !alive && !done);
+    while (need) {
+      if (chunk_next >= chunk_end) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(&lp.ctl->next_photon, (unsigned long long)lp.chunk);
+        base = __shfl_sync(kFull, base, 0);
+        if ((long long)base >= total) {
+          if (!alive) done = true;
+          break;
+        }
+        chunk_next = (long long)base;
+        chunk_end = min(chunk_next + (long long)lp.chunk, total);
+      }
+      const long long avail = chunk_end - chunk_next;
+      const int rank = __popc(need & lt_mask);
+      if (((need >> lane) & 1u) && rank < avail) {
+        const long long p = chunk_next + rank;
+        J = lp.jobs + (lp.njobs > 1 ? find_job(lp, p) : 0);
+        const long long q = p - J->pbegin;
+        start_rng<R>(rng, *J, q);
+        s.launch(*J, rng, q);
+        alive = true;
+      }
+      chunk_next += min((long long)__popc(need), avail);
+      need = __ballot_sync(kFull, !alive && !done);
+    }
+    if (__all_sync(kFull, done)) break;
+    if (alive) {
+      const int r = s.step(*J, rng, lp.max_steps);
+      if (r == kScattered) { n_steps++; n_scat++; }
+      else if (r == kAlive) { n_steps++; }
+      else {
+        if (r == kDied) n_steps++;
+        alive = false;
+        n_done++;
+      }
+    }
+  }
+  unsigned long long a = n_steps, b = n_scat, c = n_done;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(kFull, a, o);
+    b += __shfl_xor_sync(kFull, b, o);
+    c += __shfl_xor_sync(kFull, c, o);
+  }
+  if (lane == 0) {
+    atomicAdd(&lp.ctl->steps, a);
+    atomicAdd(&lp.ctl->scatters, b);
+    atomicAdd(&lp.ctl->done_photons, c);
+  }
+}
+
+}  // namespace vmc

@@ -1,0 +1,161 @@
+// walk_common.cuh -- pieces shared by the 2D and 3D photon walkers: job access, tracing,
+// photon launch from a precomputed emitting face, and counters.
+#pragma once
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "rng.cuh"
+#include "vmc_types.hpp"
+
+namespace vmc {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kMaxRejections = 4096;   // bound on launch-direction rejection loops
+
+// ---- replay trace (tape variant only) ----
+struct NoTrace {
+  __device__ __forceinline__ void begin(const JobDev &, int64_t) {}
+  __device__ __forceinline__ void put(int64_t) {}
+  __device__ __forceinline__ void end() {}
+};
+
+struct Trace {
+  int64_t *p, *len;
+  int64_t n, cap;
+  bool on;
+  __device__ __forceinline__ void begin(const JobDev &J, int64_t q) {
+    on = J.trace_on && q < J.trace_photons;
+    if (on) { p = J.trace + q * J.trace_stride; len = J.trace_len + q; cap = J.trace_stride; n = 0; }
+  }
+  __device__ __forceinline__ void put(int64_t ev) {
+    if (on) { if (n < cap) p[n] = ev; n++; }
+  }
+  __device__ __forceinline__ void end() {
+    if (on) {
+      if (n > cap) { p[cap - 1] = INT64_MIN + 5; n = cap; }
+      *len = n;
+      on = false;
+    }
+  }
+};
+
+constexpr int64_t kEvRoulette = INT64_MIN + 1;
+constexpr int64_t kEvLost = INT64_MIN + 2;
+constexpr int64_t kEvCapped = INT64_MIN + 3;
+constexpr int64_t kEvTapeEnd = INT64_MIN + 4;
+
+template <class R> struct TraceFor { using type = NoTrace; };
+template <> struct TraceFor<TapeRng> { using type = Trace; };
+
+__device__ __forceinline__ void job_count(const JobDev &J, int which) {
+  atomicAdd(J.jc + (blockIdx.x & (kSlots - 1)) * kJcN + which, 1ull);
+}
+__device__ __forceinline__ void job_ledger(const JobDev &J, int which, double v) {
+  atomicAdd(J.ledger + (blockIdx.x & (kSlots - 1)) * kLgN + which, v);
+}
+
+// first source with xi < CDF (cpp/3d/MC3D.hpp:1068-1070), clamped to the last source
+// (cpp/2d/MC2D.hpp:969; in 3D the reference would read one past the end at xi == 1)
+__device__ __forceinline__ int pick_source(const JobDev &J, double xi) {
+  int lo = 0, hi = J.Ns;  // first index with cdf > xi in [lo, hi]
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (xi < __ldg(J.cdf + mid)) hi = mid;
+    else lo = mid + 1;
+  }
+  return lo < J.Ns ? lo : J.Ns - 1;
+}
+
+// ---- 3D CreatePhoton (cpp/3d/MC3D.hpp:1060-1294) in double, from the face record ----
+template <class R>
+__device__ void create_photon_3d(const JobDev &J, R &rng, double pos[3], double dir[3], int &curel, int &curface) {
+  double xi = unif_closed(rng);
+  const SourceRec &S = J.src[pick_source(J, xi)];
+  curel = S.mother;
+  curface = S.curface;
+  double r1 = unif_open(rng), r2 = unif_open(rng);
+  double sr = sqrt(r1);
+#pragma unroll
+  for (int c = 0; c < 3; c++) pos[c] = (1.0 - sr) * S.v0[c] + sr * (1.0 - r2) * S.v1[c] + sr * r2 * S.v2[c];
+  const double n0 = S.n[0], n1 = S.n[1], n2 = S.n[2];
+  dir[0] = n0; dir[1] = n1; dir[2] = n2;  // 'l', and the combinations the reference leaves undefined
+  const char bt = S.type, dt = S.dirtype;
+  if (dt != 'n' && (bt == 'l' || bt == 'L')) {
+    dir[0] = S.L[0]; dir[1] = S.L[1]; dir[2] = S.L[2];
+  } else if (dt != 'n' && bt == 'p') {
+    pos[0] = S.L[0]; pos[1] = S.L[1]; pos[2] = S.L[2];
+  } else if ((dt == 'n' && bt == 'i') || (dt != 'n' && (bt == 'i' || bt == 'I'))) {
+    // rejection on the sphere, Mathworld sphere point picking (MC3D.hpp:1124-1141)
+    double rr0 = n0, rr1 = n1, rr2 = n2;
+    for (int it = 0; it < kMaxRejections; it++) {
+      double th = 2.0 * kPi * unif_halfup(rng);
+      double u = 2.0 * unif_closed(rng) - 1.0;
+      double st, ct;
+      sincos(th, &st, &ct);
+      double sq = sqrt(1.0 - u * u);
+      rr0 = sq * ct; rr1 = sq * st; rr2 = u;
+      if (n0 * rr0 + n1 * rr1 + n2 * rr2 > 0.0 || rng.exhausted()) break;
+    }
+    dir[0] = rr0; dir[1] = rr1; dir[2] = rr2;
+  } else if (bt == 'c' || bt == 'C') {
+    // cosinic: phi = asin(2U - 1), theta = 2 pi U, mapped onto the face frame (MC3D.hpp:1142-1191)
+    double phi = asin(2.0 * unif_open(rng) - 1.0);
+    double th = 2.0 * kPi * unif_closed(rng);
+    double sp, cp, st, ct;
+    sincos(phi, &sp, &cp);
+    sincos(th, &st, &ct);
+    double f0 = cp, f1 = ct * sp, f2 = st * sp;
+#pragma unroll
+    for (int c = 0; c < 3; c++) dir[c] = f0 * S.n[c] + f1 * S.e1[c] + f2 * S.e2[c];
+  }
+}
+
+// ---- 2D CreatePhoton (cpp/2d/MC2D.hpp:958-1132) ----
+template <class R>
+__device__ double gauss_angle(R &rng, double sigma, double h) {
+  double xi = unif_open(rng);
+  double a = -kPi / 2, b = kPi / 2, phi = 0.0;
+  const double isq2 = sqrt(2.0);
+  for (int it = 0; it < 16; it++) {
+    phi = (a + b) / 2.0;
+    double cdf = (0.5 + 0.5 * erf(phi / sigma / isq2) - h) / (1 - 2.0 * h);
+    if (cdf - xi < 0.0) a = phi;
+    else b = phi;
+  }
+  return phi;
+}
+
+template <class R>
+__device__ void create_photon_2d(const JobDev &J, R &rng, double pos[2], double dir[2], int &curel, int &curface) {
+  double xi = unif_closed(rng);
+  const SourceRec &S = J.src[pick_source(J, xi)];
+  curel = S.mother;
+  curface = S.curface;
+  double wv = unif_open(rng);
+  pos[0] = S.v0[0] + wv * (S.v1[0] - S.v0[0]);
+  pos[1] = S.v0[1] + wv * (S.v1[1] - S.v0[1]);
+  const double n0 = S.n[0], n1 = S.n[1];
+  dir[0] = n0; dir[1] = n1;
+  const char bt = S.type, dt = S.dirtype;
+  if (bt == 'l') {
+    if (dt != 'n') { dir[0] = S.L[0]; dir[1] = S.L[1]; }
+  } else if (bt == 'i') {
+    double phi = kPi * (unif_open(rng) - 0.5);
+    sincos(S.phi0 + phi, &dir[1], &dir[0]);
+  } else if (bt == 'c' || bt == 'g') {
+    // direction type 'n': one draw; otherwise redraw until the direction points inward
+    // (MC2D.hpp:1085-1124)
+    for (int it = 0; it < kMaxRejections; it++) {
+      double phi = (bt == 'c') ? asin(2.0 * unif_open(rng) - 1.0) : gauss_angle(rng, S.sigma, S.gauss_h);
+      sincos(S.phi0 + phi, &dir[1], &dir[0]);
+      if (dt == 'n' || n0 * dir[0] + n1 * dir[1] > 0.0 || rng.exhausted()) break;
+    }
+  }
+}
+
+__device__ __forceinline__ void add_d(double *p, double v) {
+  if (v != 0.0) atomicAdd(p, v);
+}
+
+}  // namespace vmc
