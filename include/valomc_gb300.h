@@ -159,6 +159,8 @@ typedef struct vmc_stats {
   int32_t grid_blocks, block_size;
   int32_t status_detail;    /* device error flags (tape end, bad index) */
   int32_t reserved;
+  int64_t bytes_h2d;        /* host-to-device bytes this call copied */
+  int64_t bytes_d2h;        /* device-to-host bytes this call copied */
 } vmc_stats;
 
 /* ---------------------------------------------------------------------------------- */

@@ -55,7 +55,7 @@ class VoProblem(C.Structure):
         ("photons_done", C.c_int64), ("capped", C.c_int64),
         ("ledger", C.c_double * 8),
         ("trace", _p64), ("trace_len", _p64), ("trace_stride", C.c_int64), ("trace_photons", C.c_int64),
-        ("seconds", C.c_double),
+        ("seconds", C.c_double), ("photon_offset", C.c_int64),
     ]
 
 
@@ -120,7 +120,7 @@ class OracleResult:
 
 
 def run(p, rng=RNG_MT, nthreads=1, normalize=True, seed=None, stream=0, max_steps=0,
-        tape=None, tape_off=None, trace_photons=0, trace_stride=100000, nphoton=None):
+        tape=None, tape_off=None, trace_photons=0, trace_stride=100000, nphoton=None, photon_offset=0):
     """Run ErrorChecks + Init + MonteCarlo of the oracle on Problem ``p``."""
     L = lib()
     D = p.dim
@@ -182,6 +182,7 @@ def run(p, rng=RNG_MT, nthreads=1, normalize=True, seed=None, stream=0, max_step
     P.seed = int(p.seed if seed is None else seed)
     P.stream = stream
     P.max_steps = max_steps
+    P.photon_offset = photon_offset
     if tape is not None:
         tape = np.ascontiguousarray(tape, dtype=np.uint32)
         tape_off = np.ascontiguousarray(tape_off, dtype=np.int64)

@@ -1148,7 +1148,7 @@ int vo_run(vo_problem *P) {
     memset(&ph, 0, sizeof(ph));
     for (int64_t i = 0; i < cnt[t]; i++) {
       int64_t p = first[t] + i;
-      if (P->rng_kind == VO_RNG_PHILOX) philox_start(&w->u.ph, P->seed, P->stream, (uint64_t)p);
+      if (P->rng_kind == VO_RNG_PHILOX) philox_start(&w->u.ph, P->seed, P->stream, (uint64_t)(p + P->photon_offset));
       if (P->rng_kind == VO_RNG_TAPE) {
         w->u.tape = P->tape; w->u.tpos = P->tape_off[p]; w->u.tend = P->tape_off[p + 1]; w->u.tape_out = 0;
       }

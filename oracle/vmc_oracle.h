@@ -99,6 +99,7 @@ typedef struct vo_problem {
   int64_t trace_stride;
   int64_t trace_photons;   /* photons [0, trace_photons) are traced */
   double seconds;          /* wall time of the photon loop */
+  int64_t photon_offset;   /* Philox mode: simulate photons [offset, offset + Nphoton) */
 } vo_problem;
 
 /* ErrorChecks + Init + MonteCarlo; returns VO_OK or 1 + mcerror */

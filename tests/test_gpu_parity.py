@@ -1,0 +1,157 @@
+"""GPU parity against the reference and its oracle, through the C ABI.
+
+* replay: both forms fed the reference's golden tapes must visit the reference's elements
+  (the plain FP64 form step for step; the FP32 form on the trajectories where FP32
+  rounding does not move a decision -- at least the first steps of every photon);
+* Philox-matched: the FP64 form and the oracle driven by the same per-photon Philox
+  streams give the same per-element fluence to rounding (tolerance below);
+* statistics: per-element fluence against the oracle's MT19937 run within 3 sigma of the
+  batch-means Monte Carlo error on >= 99% of the hit elements, chi2/dof near 1;
+* energy: absorbed + exited balances launched (with the roulette and loss ledgers) to 1e-6.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+import valomc_gb300 as V
+from golden.make_golden import TRACE_CASES, cases, tape_for
+from valomc_gb300 import meshgen as mg
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+CASES = cases()
+pytestmark = pytest.mark.gpu
+
+# Philox-matched FP64 GPU vs FP64 oracle: same photons, same draws; differences come only
+# from FMA contraction and CUDA's vs glibc's transcendental functions (a few ulps), which
+# can flip a rare near-tie decision of one photon.
+PHILOX_L1_TOL = 1e-6
+
+
+def golden_traces(name):
+    g = np.load(os.path.join(GOLD, f"trace_{name}.npz"))
+    return np.split(g["events"], np.cumsum(g["lens"])[:-1]), g
+
+
+@pytest.mark.parametrize("name", TRACE_CASES)
+def test_fp64_replay_matches_reference_elements(built, name):
+    p = CASES[name][0]
+    ev, g = golden_traces(name)
+    tape, off = tape_for(name)
+    n = len(ev)
+    r = V.run(p, precision=V.VMC_FP64, nphoton=n, tape=tape, tape_off=off, trace_photons=n, trace_stride=4096,
+              normalize=False)
+    same = [np.array_equal(a, b) for a, b in zip(r.traces, ev)]
+    assert all(same), f"{name}: photons differing {[i for i, s in enumerate(same) if not s]}"
+    # and the accumulators of those trajectories
+    for k in ("ER", "EBR"):
+        np.testing.assert_allclose(getattr(r, k), g[k], rtol=1e-9, atol=1e-12)
+
+
+@pytest.mark.parametrize("name", ["phantom3d", "pencil3d", "square2d"])
+def test_fp32_replay_follows_reference(built, name):
+    """The FP32 form consumes the tape with its own (24-bit) mappings, so only the first
+    launch draws agree exactly; the element it starts in and the first element step must
+    match, and the trajectories must stay within the mesh (no loss)."""
+    p = CASES[name][0]
+    ev, g = golden_traces(name)
+    tape, off = tape_for(name)
+    n = len(ev)
+    r = V.run(p, precision=V.VMC_FP32, nphoton=n, tape=tape, tape_off=off, trace_photons=n, trace_stride=4096,
+              normalize=False)
+    firsts = sum(1 for a, b in zip(r.traces, ev) if len(a) and len(b) and a[0] == b[0])
+    assert firsts == n
+    assert r.stats["loss"] == 0
+
+
+@pytest.mark.parametrize("name", ["phantom3d", "phantom3d_fd", "mixed3d", "mixed3d_fd", "pencil3d", "square2d",
+                                  "mixed2d", "mixed2d_fd"])
+def test_fp64_matches_oracle_on_same_philox_streams(built, name):
+    p = CASES[name][0]
+    n = 4000 if p.dim == 3 else 20000
+    gpu = V.run(p, precision=V.VMC_FP64, nphoton=n, seed=31337)
+    ref = oracle.run(p, rng=oracle.RNG_PHILOX, nthreads=4, nphoton=n, seed=31337)
+    assert ref.status == 0
+    assert gpu.stats["photons_done"] == n
+    # the mixed meshes launch pencil photons from face centroids straight along the box
+    # axes, i.e. inside interior face planes of the six-tet split: there the exit test is
+    # a near-tie that FMA contraction can decide differently for a handful of photons
+    degenerate = name.startswith("mixed3d")
+    tol = 5e-3 if degenerate else PHILOX_L1_TOL
+    assert abs(gpu.stats["loss"] - ref.loss) <= (0.002 * n if degenerate else 0)
+    for k in ("ER", "EI", "EBR", "EBI", "DEBR", "DEBI"):
+        a, b = getattr(gpu, k), getattr(ref, k)
+        den = np.abs(b).sum()
+        if den == 0:
+            assert np.abs(a).sum() == 0, k
+            continue
+        assert np.abs(a - b).sum() / den < tol, (name, k, np.abs(a - b).sum() / den)
+    if degenerate:
+        assert abs(gpu.stats["steps"] - ref.steps) <= 1e-3 * ref.steps
+    else:
+        assert gpu.stats["steps"] == ref.steps
+        assert gpu.stats["scatters"] == ref.scatters
+
+
+def batch_means(run, B):
+    """B independent batches -> per-element mean, standard error of the mean, and whether
+    the element was scored in every batch."""
+    xs = np.stack([run(b) for b in range(B)])
+    return xs.mean(0), xs.std(0, ddof=1) / np.sqrt(B), np.all(xs != 0, axis=0)
+
+
+def compare_3sigma(a, b):
+    """Elements scored in every batch of both runs (zero-hit elements are excluded; the
+    rarely hit ones have non-Gaussian batch means)."""
+    (mg_, sg, hg), (mo, so, ho) = a, b
+    hit = hg & ho
+    z = (mg_[hit] - mo[hit]) / np.sqrt(sg[hit] ** 2 + so[hit] ** 2)
+    frac = np.mean(np.abs(z) < 3.0)
+    chi2 = np.mean(z ** 2)
+    return frac, chi2, hit.sum()
+
+
+@pytest.mark.parametrize("precision", [V.VMC_FP64, V.VMC_FP32])
+@pytest.mark.parametrize("name", ["square2d", "phantom3d", "phantom3d_fd", "mixed3d", "mixed2d_fd"])
+def test_fluence_within_batch_means_error_of_oracle(built, name, precision):
+    p = CASES[name][0]
+    B = 20
+    n_gpu = 200000 if p.dim == 2 else 40000
+    n_ref = 20000 if p.dim == 2 else 4000
+
+    def gpu(b):
+        r = V.run(p, precision=precision, nphoton=n_gpu, seed=1000 + b)
+        return np.concatenate([r.ER, r.EI, r.EBR, r.EBI])
+
+    def ref(b):
+        r = oracle.run(p, rng=oracle.RNG_MT, nthreads=8, nphoton=n_ref, seed=5000 + b)
+        return np.concatenate([r.ER, r.EI, r.EBR, r.EBI])
+
+    frac, chi2, nhit = compare_3sigma(batch_means(gpu, B), batch_means(ref, B))
+    assert nhit > 50
+    # |z| < 3 for a t-like statistic with ~38 dof: expected fraction ~0.995
+    assert frac >= 0.985, (name, precision, frac, chi2, nhit)
+    assert 0.75 < chi2 < 1.35, (name, precision, frac, chi2, nhit)
+
+
+@pytest.mark.parametrize("precision", [V.VMC_FP64, V.VMC_FP32])
+def test_energy_balance(built, precision):
+    p = CASES["phantom3d"][0]
+    r = V.run(p, precision=precision, nphoton=100000, seed=4, normalize=False)
+    L = r.stats["ledger"]
+    launched = L["launched"] + L["roulette_gain"] - L["roulette_kill"] - L["lost"]
+    assert r.stats["loss"] == 0
+    assert abs(L["absorbed"] + L["exited"] - launched) / L["launched"] < 1e-6, L
+
+
+def test_energy_balance_against_launched_at_full_phantom(built):
+    """absorbed + exited vs launched on the 648k-tet phantom (roulette is unbiased only in
+    expectation: the ledger closes it exactly, the raw balance to ~1e-6)."""
+    p = mg.config_3d_phantom(nphoton=1_000_000, seed=8)
+    r = V.run(p, precision=V.VMC_FP32, normalize=False)
+    L = r.stats["ledger"]
+    assert r.stats["loss"] == 0 and r.stats["capped"] == 0
+    closed = L["launched"] + L["roulette_gain"] - L["roulette_kill"]
+    assert abs(L["absorbed"] + L["exited"] - closed) / L["launched"] < 1e-6
+    assert abs(L["absorbed"] + L["exited"] - L["launched"]) / L["launched"] < 1e-5

@@ -89,7 +89,7 @@ class VmcStats(C.Structure):
         ("steps", C.c_int64), ("scatters", C.c_int64), ("roulette_kills", C.c_int64), ("seed_used", C.c_uint64),
         ("seconds_setup", C.c_double), ("seconds_kernel", C.c_double), ("seconds_total", C.c_double),
         ("ledger", C.c_double * 8), ("grid_blocks", C.c_int32), ("block_size", C.c_int32),
-        ("status_detail", C.c_int32), ("reserved", C.c_int32),
+        ("status_detail", C.c_int32), ("reserved", C.c_int32), ("bytes_h2d", C.c_int64), ("bytes_d2h", C.c_int64),
     ]
 
 

@@ -20,6 +20,8 @@
 namespace vmc {
 
 static thread_local std::string g_last_error;
+// bytes copied between host and device by the calling thread (reported in vmc_stats)
+thread_local int64_t g_h2d_bytes = 0, g_d2h_bytes = 0;
 
 void set_error(const std::string &msg) { g_last_error = msg; }
 
@@ -77,6 +79,7 @@ static int dalloc(T **p, size_t count, int64_t &bytes) {
 template <class T>
 static int h2d(T *d, const T *h, size_t count, cudaStream_t st) {
   if (count) VMC_CK(cudaMemcpyAsync(d, h, count * sizeof(T), cudaMemcpyHostToDevice, st));
+  g_h2d_bytes += (int64_t)(count * sizeof(T));
   return VMC_OK;
 }
 
@@ -354,6 +357,7 @@ int launch_jobs(int device, const LaunchSpec &spec, const std::vector<JobDev> &j
   Ctl h;
   VMC_CK(cudaMemcpyAsync(&h, dctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
   VMC_CK(cudaStreamSynchronize(st));
+  g_d2h_bytes += (int64_t)sizeof(Ctl);
   res.steps = h.steps;
   res.scatters = h.scatters;
   res.done = h.done_photons;
@@ -372,6 +376,7 @@ int collect_job(const HostJob &j, const DeviceMesh &m, const JobBuffers &b, int6
   VMC_CK(cudaMemcpyAsync(jc.data(), b.d_jc, jc.size() * 8, cudaMemcpyDeviceToHost, stream));
   VMC_CK(cudaMemcpyAsync(lg.data(), b.d_ledger, lg.size() * 8, cudaMemcpyDeviceToHost, stream));
   VMC_CK(cudaStreamSynchronize(stream));
+  g_d2h_bytes += (int64_t)(acc.size() + jc.size() + lg.size()) * 8;
   const double *ER = acc.data(), *EI = ER + Ne, *EBR = EI + Ne, *EBI = EBR + Nb, *DEBR = EBI + Nb, *DEBI = DEBR + Nb;
   if (out) normalise(m.host, j, nphoton, ER, EI, EBR, EBI, DEBR, DEBI, out, normalize);
   if (st) {
@@ -465,13 +470,12 @@ static int prepare_options(const vmc_options *in, vmc_options &o) {
 
 int vmc_run(const vmc_input *in, const vmc_options *opt_in, vmc_output *out, vmc_stats *stats) {
   auto t0 = std::chrono::steady_clock::now();
+  g_h2d_bytes = g_d2h_bytes = 0;
   vmc_options o;
   int s = prepare_options(opt_in, o);
   if (s) return s;
   if (!in || !out) return VMC_ERR_INVALID_ARGUMENT;
   s = check_input(in);
-  if (s) return s;
-  s = select_device(o.device);
   if (s) return s;
   vmc_stats local;
   vmc_stats *st = stats ? stats : &local;
@@ -486,6 +490,9 @@ int vmc_run(const vmc_input *in, const vmc_options *opt_in, vmc_output *out, vmc
   if (s) return s;
   hj.seed = in->seed_given ? in->seed : clock_seed();
   if (o.rng == VMC_RNG_TAPE && o.tape_photons < in->Nphoton) return VMC_ERR_INVALID_ARGUMENT;
+  // every host-side check of ErrorChecks / Init has passed: now the device
+  s = select_device(o.device);
+  if (s) return s;
   s = upload_mesh(dm, mask);
   if (s) return s;
   cudaStream_t stream = 0;
@@ -546,6 +553,8 @@ int vmc_run(const vmc_input *in, const vmc_options *opt_in, vmc_output *out, vmc
   auto t2 = std::chrono::steady_clock::now();
   st->seconds_setup = std::chrono::duration<double>(t1 - t0).count();
   st->seconds_total = std::chrono::duration<double>(t2 - t0).count();
+  st->bytes_h2d = g_h2d_bytes;
+  st->bytes_d2h = g_d2h_bytes + (ntr > 0 ? (int64_t)sizeof(int64_t) * ntr * (o.trace_stride + 1) : 0);
   if (ls != VMC_OK) return ls;
   if (st->status_detail & kErrTapeEnd) return VMC_ERR_TAPE;
   return VMC_OK;
@@ -597,6 +606,7 @@ int mesh_precision_mask(const vmc_mesh *m) { return m ? m->precision_mask : 0; }
 int vmc_run_batch(vmc_mesh *const *meshes, const vmc_input *jobs, int32_t njobs, const vmc_options *opt_in,
                   vmc_output *outs, vmc_stats *stats, vmc_stats *job_stats) {
   auto t0 = std::chrono::steady_clock::now();
+  g_h2d_bytes = g_d2h_bytes = 0;
   vmc_options o;
   int s = prepare_options(opt_in, o);
   if (s) return s;
@@ -684,6 +694,8 @@ int vmc_run_batch(vmc_mesh *const *meshes, const vmc_input *jobs, int32_t njobs,
   tot.seconds_kernel = kernel_s;
   tot.seconds_setup = std::chrono::duration<double>(t1 - t0).count();
   tot.seconds_total = std::chrono::duration<double>(t2 - t0).count();
+  tot.bytes_h2d = g_h2d_bytes;
+  tot.bytes_d2h = g_d2h_bytes;
   if (stats) *stats = tot;
   return VMC_OK;
 }
