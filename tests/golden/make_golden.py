@@ -37,8 +37,11 @@ def mixed_3d(seed=1, nphoton=3000, f=0.0):
     for bad in (ord("L"), ord("I")):  # the reference leaves these undefined with type 'n'
         dtype[(types == bad) & (dtype == ord("n"))] = ord("a")
     bcl = rng.normal(size=(nb, 3))
-    cen = r[BH].mean(1)
-    bcl[types == ord("p")] = cen[types == ord("p")]
+    # pencil points inside their triangles but off the centroid: an axis-aligned ray from a
+    # face centroid of this grid runs inside an interior face plane of the six-tet split
+    w = np.array([0.2, 0.3, 0.5])
+    pts = np.einsum("k,ikc->ic", w, r[BH])
+    bcl[types == ord("p")] = pts[types == ord("p")]
     return mg.Problem(dim=3, H=H, BH=BH, r=r, mua=rng.uniform(0.01, 0.5, ne), mus=rng.uniform(0, 5, ne),
                       g=rng.uniform(0, .95, ne), n=rng.uniform(1.0, 1.5, ne), BCType=types,
                       BCn=rng.uniform(0, 1.5, nb), BCLNormal=bcl, BCLightDirectionType=dtype,

@@ -125,7 +125,9 @@ def test_fluence_within_batch_means_error_of_oracle(built, name, precision):
         return np.concatenate([r.ER, r.EI, r.EBR, r.EBI])
 
     def ref(b):
-        r = oracle.run(p, rng=oracle.RNG_MT, nthreads=8, nphoton=n_ref, seed=5000 + b)
+        # thread t of a run uses MT seed (seed + t): space the batches' seeds apart so no two
+        # batches share a stream
+        r = oracle.run(p, rng=oracle.RNG_MT, nthreads=8, nphoton=n_ref, seed=5000 + 1000 * b)
         return np.concatenate([r.ER, r.EI, r.EBR, r.EBI])
 
     frac, chi2, nhit = compare_3sigma(batch_means(gpu, B), batch_means(ref, B))

@@ -1,0 +1,146 @@
+"""Batched launches, the serving loop, cancellation / timeout, progress, and the drop-in
+executables, on the GPU through the C ABI."""
+import os
+import subprocess
+import tempfile
+import threading
+import time
+
+import numpy as np
+import pytest
+
+import valomc_gb300 as V
+from golden.make_golden import cases
+from valomc_gb300 import build as vbuild
+from valomc_gb300 import meshgen as mg
+
+pytestmark = pytest.mark.gpu
+RTOL = 1e-9  # same photons, same draws: only the order of the FP64 atomic additions differs
+
+
+def small_jobs():
+    c = cases()
+    jobs = [c["phantom3d"][0].copy(Nphoton=30000, seed=21), c["pencil3d"][0].copy(Nphoton=20000, seed=22),
+            mg.pencil_box(10, 0.03, 8.0, 0.9, 1.37, (4.3, 5.2), 25000, seed=23),
+            mg.pencil_box(14, 0.08, 15.0, 0.85, 1.41, (6.6, 2.3), 15000, seed=24)]
+    return jobs
+
+
+@pytest.mark.parametrize("precision", [V.VMC_FP64, V.VMC_FP32])
+def test_batch_equals_individual_runs(built, precision):
+    jobs = small_jobs()
+    meshes = [V.Mesh(p, precision=precision) for p in jobs]
+    res, tot = V.run_batch(meshes, jobs, precision=precision)
+    assert tot["photons_done"] == sum(p.Nphoton for p in jobs)
+    for p, r in zip(jobs, res):
+        one = V.run(p, precision=precision)
+        np.testing.assert_allclose(r.ER, one.ER, rtol=RTOL, atol=1e-300)
+        np.testing.assert_allclose(r.EBR, one.EBR, rtol=RTOL, atol=1e-300)
+
+
+def test_autotuner_returns_a_valid_shape(built):
+    jobs = small_jobs()
+    meshes = [V.Mesh(p) for p in jobs]
+    o = V.autotune(meshes, jobs, budget_s=1.0)
+    assert o.block_size in (64, 128, 256) and o.fetch_chunk in (32, 64, 128)
+    res, _ = V.run_batch(meshes, jobs, opts=o)
+    assert all(r.ER.sum() > 0 for r in res)
+
+
+@pytest.mark.parametrize("precision", [V.VMC_FP64, V.VMC_FP32])
+def test_server_result_alone_equals_result_in_the_mix(built, precision):
+    jobs = small_jobs()
+    meshes = [V.Mesh(p, precision=precision) for p in jobs]
+    # alone: one request at a time, small epochs so requests are sliced across launches
+    srv = V.Server(precision=precision, max_slots=8, memory_budget=1 << 30, epoch_photons=7000)
+    ids = [srv.add_mesh(m) for m in meshes]
+    alone = []
+    for k, p in enumerate(jobs):
+        rid = srv.submit(ids[k], p)
+        alone.append(srv.wait(rid))
+    # mixed: everything in flight together, submitted while others run
+    rids = [srv.submit(ids[k], p) for k, p in enumerate(jobs)]
+    mixed = [srv.wait(r) for r in rids]
+    srv.close()
+    for p, a, m in zip(jobs, alone, mixed):
+        one = V.run(p, precision=precision)
+        np.testing.assert_allclose(a.ER, m.ER, rtol=RTOL, atol=1e-300)
+        np.testing.assert_allclose(a.ER, one.ER, rtol=RTOL, atol=1e-300)
+        np.testing.assert_allclose(m.EBR, one.EBR, rtol=RTOL, atol=1e-300)
+        assert m.stats["photons_done"] == p.Nphoton
+
+
+def test_server_admission_by_memory_footprint(built):
+    p = cases()["phantom3d"][0]
+    mesh = V.Mesh(p)
+    srv = V.Server(max_slots=4, memory_budget=200_000)  # smaller than one request's state
+    mid = srv.add_mesh(mesh)
+    rid = srv.submit(mid, p, nphoton=1000)
+    with pytest.raises(V.VmcError) as e:
+        srv.wait(rid, timeout_s=30)
+    assert e.value.status == 39  # VMC_ERR_ADMISSION
+    srv.close()
+
+
+def test_server_poll_before_finish(built):
+    p = mg.config_3d_phantom(nphoton=1, seed=2)
+    mesh = V.Mesh(p)
+    srv = V.Server(max_slots=4, memory_budget=1 << 30)
+    mid = srv.add_mesh(mesh)
+    rid = srv.submit(mid, p, nphoton=5_000_000)
+    assert srv.poll(rid) is None
+    r = srv.wait(rid, timeout_s=120)
+    assert r is not None and r.stats["photons_done"] == 5_000_000
+    assert r.stats["seconds_total"] >= r.stats["seconds_kernel"] > 0
+    srv.close()
+
+
+def test_timeout_stops_the_kernel_and_the_context_stays_usable(built):
+    p = mg.config_3d_phantom(nphoton=2_000_000_000, seed=3)
+    t0 = time.time()
+    r = V.run(p, check=False, timeout_s=0.5)
+    assert r.stats["status"] == 37  # VMC_ERR_TIMEOUT
+    assert time.time() - t0 < 30
+    assert 0 < r.stats["photons_done"] < p.Nphoton
+    ok = V.run(cases()["phantom3d"][0], nphoton=1000)
+    assert ok.stats["photons_done"] == 1000
+
+
+def test_cancel_flag_and_progress_callback(built):
+    p = mg.config_3d_phantom(nphoton=2_000_000_000, seed=4)
+    flag = np.zeros(1, np.int32)
+    threading.Timer(0.4, lambda: flag.__setitem__(0, 1)).start()
+    r = V.run(p, check=False, cancel=flag)
+    assert r.stats["status"] == 36  # VMC_ERR_CANCELLED
+    seen = []
+
+    def prog(pct):
+        seen.append(pct)
+        return len(seen) < 3  # abort at the third report, like the MEX waitbar's cancel
+
+    r = V.run(p, check=False, progress=prog)
+    assert r.stats["status"] == 36 and len(seen) == 3
+    assert all(0 <= s <= 100 for s in seen)
+
+
+@pytest.mark.parametrize("dim", [3, 2])
+def test_executable_writes_the_reference_format(built, dim):
+    p = cases()["phantom3d" if dim == 3 else "square2d"][0].copy(Nphoton=20000, seed=77)
+    exe = os.path.join(vbuild.BUILD, f"MC{dim}D")
+    with tempfile.TemporaryDirectory() as td:
+        fin, fout = os.path.join(td, "in.txt"), os.path.join(td, "out.txt")
+        mg.write_input(fin, p)
+        res = subprocess.run([exe, fin, fout] + (["-s"] if dim == 2 else []), capture_output=True, text=True,
+                             timeout=300)
+        assert res.returncode == 0, res.stdout + res.stderr
+        assert "Computation took" in res.stdout
+        lines = open(fout).read().splitlines()
+    assert len(lines) == 1 + p.Ne + p.Nb
+    assert lines[0].endswith(" 0")
+    if dim == 3:
+        assert len(lines[1]) == 37  # "%18.10e %18.10e"
+    vals = np.array([[float(x) for x in ln.split()] for ln in lines[1:]])
+    one = V.run(p)
+    rt = 1e-9 if dim == 3 else 1e-5
+    np.testing.assert_allclose(vals[:p.Ne, 0], one.ER, rtol=rt, atol=1e-300)
+    np.testing.assert_allclose(vals[p.Ne:, 0], one.EBR, rtol=rt, atol=1e-300)

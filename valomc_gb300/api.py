@@ -122,9 +122,10 @@ def lib(build_if_missing=True):
     """The loaded native library (built on first use when missing)."""
     global _lib
     if _lib is None:
-        if not os.path.exists(_build.LIB) and build_if_missing:
+        path = os.environ.get("VALOMC_GB300_LIB", _build.LIB)  # an alternative build of the library
+        if path == _build.LIB and not os.path.exists(path) and build_if_missing:
             _build.build()
-        L = C.CDLL(_build.LIB)
+        L = C.CDLL(path)
         L.vmc_status_string.restype = C.c_char_p
         L.vmc_status_string.argtypes = [C.c_int]
         L.vmc_last_error.restype = C.c_char_p

@@ -40,6 +40,8 @@ struct JobBuffers {
   uint8_t *d_bctype = nullptr;
   double *d_bcn = nullptr, *d_cdf = nullptr;
   SourceRec *d_src = nullptr;
+  float *d_cdf_f = nullptr;
+  SourceRecF *d_src_f = nullptr;
   double *d_acc = nullptr;  // ER, EI [Ne]; EBR, EBI, DEBR, DEBI [Nb]
   unsigned long long *d_jc = nullptr;
   double *d_ledger = nullptr;

@@ -515,6 +515,21 @@ int build_job(const vmc_input *in, const HostMesh &m, HostJob &j) {
   const double tot = j.cdf[ns - 1];
   for (size_t i = 0; i < ns; i++) j.cdf[i] /= tot;
   if (!(j.cdf[ns - 1] == j.cdf[ns - 1])) return E_NO_LIGHTSOURCE;  // zero total weight
+  j.src_f.resize(ns);
+  j.cdf_f.resize(ns);
+  for (size_t i = 0; i < ns; i++) {
+    const SourceRec &S = j.src[i];
+    SourceRecF &F = j.src_f[i];
+    memset(&F, 0, sizeof(F));
+    for (int c = 0; c < 3; c++) {
+      F.v0[c] = (float)S.v0[c]; F.v1[c] = (float)S.v1[c]; F.v2[c] = (float)S.v2[c];
+      F.n[c] = (float)S.n[c]; F.e1[c] = (float)S.e1[c]; F.e2[c] = (float)S.e2[c]; F.L[c] = (float)S.L[c];
+    }
+    F.phi0 = (float)S.phi0; F.sigma = (float)S.sigma; F.gauss_h = (float)S.gauss_h;
+    F.mother = S.mother; F.curface = S.curface; F.ib = S.ib; F.type = S.type; F.dirtype = S.dirtype;
+    j.cdf_f[i] = (float)j.cdf[i];
+  }
+  j.cdf_f[ns - 1] = 1.0f;
   return VMC_OK;
 }
 

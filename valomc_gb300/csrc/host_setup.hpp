@@ -41,6 +41,8 @@ struct HostJob {
   std::vector<double> bcn;
   std::vector<SourceRec> src;
   std::vector<double> cdf;
+  std::vector<SourceRecF> src_f;  // FP32 copies for the tracking form
+  std::vector<float> cdf_f;
   double f = 0, omega = 0, k_scale = 0, phase0 = 0;
   int64_t Nphoton = 0;
   uint64_t seed = 0;

@@ -32,7 +32,7 @@ __device__ __forceinline__ int find_job(const LaunchParams &lp, int64_t p) {
 }
 
 template <class W, class R>
-__global__ void __launch_bounds__(256) pool_kernel(const LaunchParams lp) {
+__global__ void __launch_bounds__(256, W::kMinBlocks) pool_kernel(const LaunchParams lp) {
   W s;
   R rng;
   const JobDev *J = lp.jobs;

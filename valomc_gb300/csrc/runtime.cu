@@ -140,17 +140,19 @@ int upload_mesh(DeviceMesh &m, int precision_mask) {
 JobBuffers::~JobBuffers() { release(); }
 
 void JobBuffers::release() {
-  void *ps[] = {d_optics, d_bctype, d_bcn, d_cdf, d_src, d_acc, d_jc, d_ledger, d_tape, d_tape_off, d_trace, d_trace_len};
+  void *ps[] = {d_optics, d_bctype, d_bcn, d_cdf, d_src, d_cdf_f, d_src_f, d_acc, d_jc, d_ledger,
+                d_tape, d_tape_off, d_trace, d_trace_len};
   for (void *p : ps)
     if (p) cudaFree(p);
   d_optics = nullptr; d_bctype = nullptr; d_bcn = d_cdf = nullptr; d_src = nullptr; d_acc = nullptr;
+  d_cdf_f = nullptr; d_src_f = nullptr;
   d_jc = nullptr; d_ledger = nullptr; d_tape = nullptr; d_tape_off = d_trace = d_trace_len = nullptr;
   bytes = 0;
 }
 
 int64_t job_footprint(const HostJob &j, const HostMesh &m) {
   const int64_t rows = j.homogeneous ? 1 : m.Ne;
-  return rows * 32 + m.Nb * 9 + (int64_t)j.src.size() * (int64_t)(sizeof(SourceRec) + 8) +
+  return rows * 32 + m.Nb * 9 + (int64_t)j.src.size() * (int64_t)(sizeof(SourceRec) + sizeof(SourceRecF) + 12) +
          (2 * m.Ne + 4 * m.Nb) * 8 + kSlots * (kJcN + kLgN) * 8;
 }
 
@@ -180,6 +182,10 @@ int upload_job(const HostJob &j, const DeviceMesh &m, int precision, JobBuffers 
   VMC_TRY(h2d(b.d_cdf, j.cdf.data(), j.cdf.size(), st));
   VMC_TRY(dalloc(&b.d_src, j.src.size(), b.bytes));
   VMC_TRY(h2d(b.d_src, j.src.data(), j.src.size(), st));
+  VMC_TRY(dalloc(&b.d_cdf_f, j.cdf_f.size(), b.bytes));
+  VMC_TRY(h2d(b.d_cdf_f, j.cdf_f.data(), j.cdf_f.size(), st));
+  VMC_TRY(dalloc(&b.d_src_f, j.src_f.size(), b.bytes));
+  VMC_TRY(h2d(b.d_src_f, j.src_f.data(), j.src_f.size(), st));
   VMC_TRY(dalloc(&b.d_acc, (size_t)(2 * Ne + 4 * Nb), b.bytes));
   VMC_TRY(dalloc(&b.d_jc, (size_t)kSlots * kJcN, b.bytes));
   VMC_TRY(dalloc(&b.d_ledger, (size_t)kSlots * kLgN, b.bytes));
@@ -205,6 +211,8 @@ JobDev describe_job(const HostJob &j, const DeviceMesh &m, int precision, const 
   d.Nb = (int32_t)Nb;
   d.cdf = b.d_cdf;
   d.src = b.d_src;
+  d.cdf_f = b.d_cdf_f;
+  d.src_f = b.d_src_f;
   d.bctype = b.d_bctype;
   d.bcn = b.d_bcn;
   d.bnorm = m.d_bnorm;

@@ -71,6 +71,18 @@ struct alignas(16) SourceRec {
   int8_t pad[2];
 };
 
+// The same face record in FP32 for the tracking form's launch (no FP64 on its hot path).
+struct alignas(16) SourceRecF {
+  float v0[3], v1[3], v2[3];
+  float n[3];
+  float e1[3], e2[3];
+  float L[3];
+  float phi0, sigma, gauss_h;
+  int32_t mother, curface, ib;
+  int8_t type, dirtype;
+  int8_t pad[2];
+};
+
 // Per-job counters written by the kernel (rare events only; steps are global).
 // Rare-event counters are spread over kSlots copies (slot = block index mod kSlots) so that
 // concurrent warps do not serialise on one address; the host sums the slots.
@@ -86,6 +98,8 @@ struct JobDev {
   int32_t Ne, Nb;
   const double *cdf;           // [Ns]
   const SourceRec *src;        // [Ns]
+  const float *cdf_f;          // [Ns] FP32 copies for the tracking form
+  const SourceRecF *src_f;     // [Ns]
   const uint8_t *bctype;       // [Nb]
   const double *bcn;           // [Nb]
   const double *bnorm;         // [Nb x 4] Normal(ib) for MirrorPhoton (FP64 forms)

@@ -24,6 +24,7 @@ __device__ __forceinline__ bool ray_seg(const double R[2], const double D[2], co
 
 template <bool FD, class R>
 struct Walk2D64 {
+  static constexpr int kMinBlocks = 1;
   using Tr = typename TraceFor<R>::type;
   double pos[2], dir[2];
   double w, prop, phase, cph, sph;
@@ -243,6 +244,7 @@ struct Walk2D64 {
 
 template <bool FD, class R>
 struct Walk2D32 {
+  static constexpr int kMinBlocks = 4;
   using Tr = typename TraceFor<R>::type;
   float px, py, dx, dy;
   float w, prop, phase;
@@ -250,6 +252,7 @@ struct Walk2D32 {
   float acc, accI;
   int el;
   int32_t nsteps;
+  bool outward;  // launched out through its own entry edge
   Tr tr;
 
   __device__ __forceinline__ float4 optics(const JobDev &J, int e) const {
@@ -258,23 +261,30 @@ struct Walk2D32 {
 
   __device__ void launch(const JobDev &J, R &rng, int64_t q) {
     tr.begin(J, q);
-    double p[2], d[2];
+    float p[2], d[2];
     int cf;
-    create_photon_2d(J, rng, p, d, el, cf);
-    px = (float)p[0]; py = (float)p[1];
-    dx = (float)d[0]; dy = (float)d[1];
+    create_photon_2d_f(J, rng, p, d, el, cf);
+    px = p[0]; py = p[1];
+    dx = d[0]; dy = d[1];
+    // the entry edge is never tested by the reference's WhichFace (MC2D.hpp:927-952): a
+    // photon launched out through it is lost
+    outward = false;
+    if (cf >= 0) {
+      const float4 ln = __ldg(reinterpret_cast<const float4 *>((reinterpret_cast<const Tri32 *>(J.geom) + el)->ln) + cf);
+      outward = ln.x * dx + ln.y * dy > 0.0f;
+    }
     w = 1.0f;
     phase = (float)J.phase0;
     float4 o = optics(J, el);
     mua = o.x; mus = o.y; g = o.z; nidx = o.w;
-    prop = -logf(unif_open_f(rng)) / mus;
+    prop = __fdividef(-logf(unif_open_f(rng)), mus);
     acc = accI = 0.0f;
     nsteps = 0;
   }
 
   __device__ __forceinline__ void flush(const JobDev &J) {
-    if (acc != 0.0f) atomicAdd(J.ER + el, (double)acc);
-    if (FD && accI != 0.0f) atomicAdd(J.EI + el, (double)accI);
+    add_f(J.ER + el, acc);
+    if (FD) add_f(J.EI + el, accI);
     acc = accI = 0.0f;
   }
 
@@ -315,8 +325,6 @@ struct Walk2D32 {
     if (boundary) return false;
     float m = copysignf(ct, dn) - eta * dn;
     dx = eta * dx + m * nx; dy = eta * dy + m * ny;
-    float in = rsqrtf(dx * dx + dy * dy);
-    dx *= in; dy *= in;
     return false;
   }
 
@@ -345,6 +353,11 @@ struct Walk2D32 {
       die(J, kEvCapped);
       return kDiedEarly;
     }
+    if (outward) {
+      job_count(J, kJcLoss); job_ledger(J, kLgLost, (double)w);
+      die(J, kEvLost);
+      return kDiedEarly;
+    }
     const Tri32 *T = reinterpret_cast<const Tri32 *>(J.geom) + el;
     const float4 *L4 = reinterpret_cast<const float4 *>(T->ln);
     const float4 l0 = __ldg(L4 + 0), l1 = __ldg(L4 + 1), l2 = __ldg(L4 + 2);
@@ -357,7 +370,7 @@ struct Walk2D32 {
       for (int f = 0; f < 3; f++) {
         float nd = ln[f].x * dx + ln[f].y * dy;
         if (nd > 0.0f) {
-          float t = (ln[f].z - (ln[f].x * px + ln[f].y * py)) / nd;
+          float t = __fdividef(ln[f].z - (ln[f].x * px + ln[f].y * py), nd);
           if (t < best) { best = t; nf = f; }
         }
       }
@@ -399,7 +412,7 @@ struct Walk2D32 {
     if (prop <= 0.0f) {
       int res = kAlive;
       if (mus > 0.0f) { scatter(rng); res = kScattered; }
-      prop = -logf(unif_open_f(rng)) / mus;
+      prop = __fdividef(-logf(unif_open_f(rng)), mus);
       return res;
     }
     const float nx = lsel(l0, l1, l2, nf, 0), ny = lsel(l0, l1, l2, nf, 1);
@@ -417,15 +430,15 @@ struct Walk2D32 {
       float dn = dx * nx + dy * ny;
       flush(J);
       if (!FD) {
-        add_d(J.EBR + ib, (double)w);
-        add_d(J.DEBR + ib, (double)w / (double)dn);
+        add_f(J.EBR + ib, w);
+        add_f(J.DEBR + ib, __fdividef(w, dn));
       } else {
         float sp, cp;
         sincosf(phase, &sp, &cp);
-        add_d(J.EBR + ib, (double)(w * cp));
-        add_d(J.EBI + ib, -(double)(w * sp));
-        add_d(J.DEBR + ib, (double)(w * cp) / (double)dn);
-        add_d(J.DEBI + ib, -(double)(w * sp) / (double)dn);
+        add_f(J.EBR + ib, w * cp);
+        add_f(J.EBI + ib, -(w * sp));
+        add_f(J.DEBR + ib, __fdividef(w * cp, dn));
+        add_f(J.DEBI + ib, -__fdividef(w * sp, dn));
       }
       tr.put(-1 - (int64_t)ib);
       tr.end();
@@ -437,7 +450,7 @@ struct Walk2D32 {
     }
     const float4 o2 = optics(J, nextel);
     if (mus <= 0.0f && o2.y > 0.0f) {
-      prop = -logf(unif_open_f(rng)) / o2.y;
+      prop = __fdividef(-logf(unif_open_f(rng)), o2.y);
       if (roulette(J, rng)) return die(J, kEvRoulette);
       if (nidx != o2.w && fresnel(rng, nx, ny, nidx / o2.w, false)) return kAlive;
     } else {

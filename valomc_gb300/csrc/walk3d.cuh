@@ -67,6 +67,10 @@ __device__ __forceinline__ bool fresnel_reflects_f(R &rng, float eta, float ci, 
   float s = 1.0f - eta * eta * (1.0f - ci * ci);
   if (s <= 0.0f) return true;
   ct = sqrtf(s);
+  // a launch direction that is not unit length (3D BCLNormal of direction type 'a'/'r' is
+  // not normalised, MC3D.hpp:679-683) can give |cos| > 1: acos is then NaN in the
+  // reference, R is NaN and the photon is transmitted
+  if (!(ci <= 1.0f)) return false;
   float rs = (eta * ci - ct) / (eta * ci + ct);
   float rp = (ci - eta * ct) / (ci + eta * ct);
   float Rf = 0.5f * (rs * rs + rp * rp);
@@ -80,6 +84,7 @@ __device__ __forceinline__ bool is_mirror(uint8_t bt) { return bt == 'm' || bt =
 // =====================================================================================
 template <bool FD, class R>
 struct Walk3D64 {
+  static constexpr int kMinBlocks = 1;  // ~125 registers: 2 CTAs of 256 per SM
   using Tr = typename TraceFor<R>::type;
   double pos[3], dir[3];
   double w, prop, phase, cph, sph;
@@ -323,6 +328,9 @@ struct Walk3D64 {
 // =====================================================================================
 template <bool FD, class R>
 struct Walk3D32 {
+  // 4 CTAs of 256 per SM (64 registers): the walk is latency bound and more resident
+  // warps beat the few spills (measured +7% over 3 CTAs on the 648k-tet phantom)
+  static constexpr int kMinBlocks = 4;
   using Tr = typename TraceFor<R>::type;
   float px, py, pz, dx, dy, dz;
   float w, prop, phase;
@@ -330,6 +338,7 @@ struct Walk3D32 {
   float acc, accI;
   int el;
   int32_t nsteps;
+  bool outward;  // launched out through its own entry face
   Tr tr;
 
   __device__ __forceinline__ float4 optics(const JobDev &J, int e) const {
@@ -338,23 +347,31 @@ struct Walk3D32 {
 
   __device__ void launch(const JobDev &J, R &rng, int64_t q) {
     tr.begin(J, q);
-    double p[3], d[3];
+    float p[3], d[3];
     int cf;
-    create_photon_3d(J, rng, p, d, el, cf);
-    px = (float)p[0]; py = (float)p[1]; pz = (float)p[2];
-    dx = (float)d[0]; dy = (float)d[1]; dz = (float)d[2];
+    create_photon_3d_f(J, rng, p, d, el, cf);
+    px = p[0]; py = p[1]; pz = p[2];
+    dx = d[0]; dy = d[1]; dz = d[2];
+    // The reference's WhichFace never tests the face a photon starts on, so a photon
+    // launched pointing out of that face finds no exit and is lost (MC3D.hpp:1020-1056,
+    // :1464-1468).  Keep that rule: the outward plane of the entry face decides.
+    outward = false;
+    if (cf >= 0) {
+      const float4 pl = __ldg(reinterpret_cast<const float4 *>((reinterpret_cast<const Tet32 *>(J.geom) + el)->pl) + cf);
+      outward = pl.x * dx + pl.y * dy + pl.z * dz > 0.0f;
+    }
     w = 1.0f;
     phase = (float)J.phase0;
     float4 o = optics(J, el);
     mua = o.x; mus = o.y; g = o.z; nidx = o.w;
-    prop = -logf(unif_open_f(rng)) / mus;
+    prop = __fdividef(-logf(unif_open_f(rng)), mus);
     acc = accI = 0.0f;
     nsteps = 0;
   }
 
   __device__ __forceinline__ void flush(const JobDev &J) {
-    if (acc != 0.0f) atomicAdd(J.ER + el, (double)acc);
-    if (FD && accI != 0.0f) atomicAdd(J.EI + el, (double)accI);
+    add_f(J.ER + el, acc);
+    if (FD) add_f(J.EI + el, accI);
     acc = accI = 0.0f;
   }
 
@@ -372,8 +389,8 @@ struct Walk3D32 {
     float ct;
     if (g != 0.0f) {
       if (xi > 0.0f && xi < 1.0f) {
-        float q = (1.0f - g * g) / (1.0f - g + 2.0f * g * xi);
-        ct = (1.0f + g * g - q * q) / (2.0f * g);
+        float q = __fdividef(1.0f - g * g, 1.0f - g + 2.0f * g * xi);
+        ct = __fdividef(1.0f + g * g - q * q, 2.0f * g);
       } else {
         ct = xi > 0.5f ? 1.0f : -1.0f;  // theta = (1 - xi) pi at xi in {0, 1}
       }
@@ -412,8 +429,6 @@ struct Walk3D32 {
     // refraction: d' = eta d + (ct - eta ci) s N with s the side the photon moves to
     float m = copysignf(ct, dn) - eta * dn;
     dx = eta * dx + m * nx; dy = eta * dy + m * ny; dz = eta * dz + m * nz;
-    float in = rsqrtf(dx * dx + dy * dy + dz * dz);
-    dx *= in; dy *= in; dz *= in;
     return false;
   }
 
@@ -437,6 +452,11 @@ struct Walk3D32 {
       die(J, kEvCapped);
       return kDiedEarly;
     }
+    if (outward) {
+      job_count(J, kJcLoss); job_ledger(J, kLgLost, (double)w);
+      die(J, kEvLost);
+      return kDiedEarly;
+    }
     const Tet32 *T = reinterpret_cast<const Tet32 *>(J.geom) + el;
     const float4 *P4 = reinterpret_cast<const float4 *>(T->pl);
     const float4 p0 = __ldg(P4 + 0), p1 = __ldg(P4 + 1), p2 = __ldg(P4 + 2), p3 = __ldg(P4 + 3);
@@ -450,7 +470,7 @@ struct Walk3D32 {
       for (int f = 0; f < 4; f++) {
         float nd = pl[f].x * dx + pl[f].y * dy + pl[f].z * dz;
         if (nd > 0.0f) {
-          float t = (pl[f].w - (pl[f].x * px + pl[f].y * py + pl[f].z * pz)) / nd;
+          float t = __fdividef(pl[f].w - (pl[f].x * px + pl[f].y * py + pl[f].z * pz), nd);
           if (t < best) { best = t; nf = f; }
         }
       }
@@ -494,7 +514,7 @@ struct Walk3D32 {
     if (prop <= 0.0f) {
       int res = kAlive;
       if (mus > 0.0f) { scatter(rng); res = kScattered; }
-      prop = -logf(unif_open_f(rng)) / mus;
+      prop = __fdividef(-logf(unif_open_f(rng)), mus);
       return res;
     }
     const float4 pf = nf == 0 ? p0 : nf == 1 ? p1 : nf == 2 ? p2 : p3;
@@ -510,12 +530,12 @@ struct Walk3D32 {
       const double bcn = __ldg(J.bcn + ib);
       if (bcn > 0.0 && fresnel(rng, pf.x, pf.y, pf.z, (float)((double)nidx / bcn))) return kAlive;
       flush(J);
-      if (!FD) add_d(J.EBR + ib, (double)w);
+      if (!FD) add_f(J.EBR + ib, w);
       else {
         float sp, cp;
         sincosf(phase, &sp, &cp);
-        add_d(J.EBR + ib, (double)(w * cp));
-        add_d(J.EBI + ib, -(double)(w * sp));
+        add_f(J.EBR + ib, w * cp);
+        add_f(J.EBI + ib, -(w * sp));
       }
       tr.put(-1 - (int64_t)ib);
       tr.end();
@@ -527,7 +547,7 @@ struct Walk3D32 {
     }
     const float4 o2 = optics(J, nextel);
     if (mus <= 0.0f && o2.y > 0.0f) {
-      prop = -logf(unif_open_f(rng)) / o2.y;
+      prop = __fdividef(-logf(unif_open_f(rng)), o2.y);
       if (roulette(J, rng)) return die(J, kEvRoulette);
       if (nidx != o2.w && fresnel(rng, pf.x, pf.y, pf.z, nidx / o2.w)) return kAlive;
     } else {

@@ -69,7 +69,7 @@ __device__ __forceinline__ int pick_source(const JobDev &J, double xi) {
 
 // ---- 3D CreatePhoton (cpp/3d/MC3D.hpp:1060-1294) in double, from the face record ----
 template <class R>
-__device__ void create_photon_3d(const JobDev &J, R &rng, double pos[3], double dir[3], int &curel, int &curface) {
+__device__ __forceinline__ void create_photon_3d(const JobDev &J, R &rng, double pos[3], double dir[3], int &curel, int &curface) {
   double xi = unif_closed(rng);
   const SourceRec &S = J.src[pick_source(J, xi)];
   curel = S.mother;
@@ -127,7 +127,7 @@ __device__ double gauss_angle(R &rng, double sigma, double h) {
 }
 
 template <class R>
-__device__ void create_photon_2d(const JobDev &J, R &rng, double pos[2], double dir[2], int &curel, int &curface) {
+__device__ __forceinline__ void create_photon_2d(const JobDev &J, R &rng, double pos[2], double dir[2], int &curel, int &curface) {
   double xi = unif_closed(rng);
   const SourceRec &S = J.src[pick_source(J, xi)];
   curel = S.mother;
@@ -156,6 +156,113 @@ __device__ void create_photon_2d(const JobDev &J, R &rng, double pos[2], double 
 
 __device__ __forceinline__ void add_d(double *p, double v) {
   if (v != 0.0) atomicAdd(p, v);
+}
+
+// float -> double by bit manipulation on the integer pipe (exact for normal floats; zero
+// and subnormal inputs give 0).  GB300's FP64 pipe is 1/64 of FP32, so the tracking form
+// keeps conversions off it.
+__device__ __forceinline__ double f2d_int(float x) {
+  const uint32_t b = __float_as_uint(x);
+  const uint32_t e = (b >> 23) & 0xffu;
+  if (e == 0u) return 0.0;
+  const uint64_t bits = ((uint64_t)(b >> 31) << 63) | ((uint64_t)(e + (1023u - 127u)) << 52) |
+                        ((uint64_t)(b & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)bits);
+}
+
+__device__ __forceinline__ void add_f(double *p, float v) {
+  if (v != 0.0f) atomicAdd(p, f2d_int(v));
+}
+
+// ---- FP32 launch for the tracking form: same draws and sampling laws as CreatePhoton,
+// evaluated in float from the FP32 face records (cos(asin(s)) = sqrt(1 - s^2)) ----
+__device__ __forceinline__ int pick_source_f(const JobDev &J, float xi) {
+  int lo = 0, hi = J.Ns;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (xi < __ldg(J.cdf_f + mid)) hi = mid;
+    else lo = mid + 1;
+  }
+  return lo < J.Ns ? lo : J.Ns - 1;
+}
+
+template <class R>
+__device__ __forceinline__ void create_photon_3d_f(const JobDev &J, R &rng, float pos[3], float dir[3], int &curel,
+                                                   int &curface) {
+  const SourceRecF &S = J.src_f[pick_source_f(J, unif_closed_f(rng))];
+  curel = S.mother;
+  curface = S.curface;
+  const float r1 = unif_open_f(rng), r2 = unif_open_f(rng);
+  const float sr = sqrtf(r1);
+#pragma unroll
+  for (int c = 0; c < 3; c++) pos[c] = (1.0f - sr) * S.v0[c] + sr * (1.0f - r2) * S.v1[c] + sr * r2 * S.v2[c];
+  const float n0 = S.n[0], n1 = S.n[1], n2 = S.n[2];
+  dir[0] = n0; dir[1] = n1; dir[2] = n2;
+  const char bt = S.type, dt = S.dirtype;
+  if (dt != 'n' && (bt == 'l' || bt == 'L')) {
+    dir[0] = S.L[0]; dir[1] = S.L[1]; dir[2] = S.L[2];
+  } else if (dt != 'n' && bt == 'p') {
+    pos[0] = S.L[0]; pos[1] = S.L[1]; pos[2] = S.L[2];
+  } else if ((dt == 'n' && bt == 'i') || (dt != 'n' && (bt == 'i' || bt == 'I'))) {
+    float rr0 = n0, rr1 = n1, rr2 = n2;
+    for (int it = 0; it < kMaxRejections; it++) {
+      const float th2 = 2.0f * unif_halfup_f(rng);  // theta / pi
+      const float u = 2.0f * unif_closed_f(rng) - 1.0f;
+      float st, ct;
+      sincospif(th2, &st, &ct);
+      const float sq = sqrtf(fmaxf(0.0f, 1.0f - u * u));
+      rr0 = sq * ct; rr1 = sq * st; rr2 = u;
+      if (n0 * rr0 + n1 * rr1 + n2 * rr2 > 0.0f || rng.exhausted()) break;
+    }
+    dir[0] = rr0; dir[1] = rr1; dir[2] = rr2;
+  } else if (bt == 'c' || bt == 'C') {
+    const float s = 2.0f * unif_open_f(rng) - 1.0f;  // sin(phi), phi = asin(2U - 1)
+    const float cphi = sqrtf(fmaxf(0.0f, 1.0f - s * s));
+    float st, ct;
+    sincospif(2.0f * unif_closed_f(rng), &st, &ct);
+    const float f0 = cphi, f1 = ct * s, f2 = st * s;
+#pragma unroll
+    for (int c = 0; c < 3; c++) dir[c] = f0 * S.n[c] + f1 * S.e1[c] + f2 * S.e2[c];
+  }
+}
+
+template <class R>
+__device__ __forceinline__ float gauss_angle_f(R &rng, float sigma, float h) {
+  const float xi = unif_open_f(rng);
+  float a = -0.5f * (float)kPi, b = 0.5f * (float)kPi, phi = 0.0f;
+  for (int it = 0; it < 16; it++) {
+    phi = 0.5f * (a + b);
+    const float cdf = (0.5f + 0.5f * erff(phi / sigma * 0.70710678118654752f) - h) / (1.0f - 2.0f * h);
+    if (cdf - xi < 0.0f) a = phi;
+    else b = phi;
+  }
+  return phi;
+}
+
+template <class R>
+__device__ __forceinline__ void create_photon_2d_f(const JobDev &J, R &rng, float pos[2], float dir[2], int &curel,
+                                                   int &curface) {
+  const SourceRecF &S = J.src_f[pick_source_f(J, unif_closed_f(rng))];
+  curel = S.mother;
+  curface = S.curface;
+  const float wv = unif_open_f(rng);
+  pos[0] = S.v0[0] + wv * (S.v1[0] - S.v0[0]);
+  pos[1] = S.v0[1] + wv * (S.v1[1] - S.v0[1]);
+  const float n0 = S.n[0], n1 = S.n[1];
+  dir[0] = n0; dir[1] = n1;
+  const char bt = S.type, dt = S.dirtype;
+  if (bt == 'l') {
+    if (dt != 'n') { dir[0] = S.L[0]; dir[1] = S.L[1]; }
+  } else if (bt == 'i') {
+    const float phi = (float)kPi * (unif_open_f(rng) - 0.5f);
+    sincosf(S.phi0 + phi, &dir[1], &dir[0]);
+  } else if (bt == 'c' || bt == 'g') {
+    for (int it = 0; it < kMaxRejections; it++) {
+      const float phi = (bt == 'c') ? asinf(2.0f * unif_open_f(rng) - 1.0f) : gauss_angle_f(rng, S.sigma, S.gauss_h);
+      sincosf(S.phi0 + phi, &dir[1], &dir[0]);
+      if (dt == 'n' || n0 * dir[0] + n1 * dir[1] > 0.0f || rng.exhausted()) break;
+    }
+  }
 }
 
 }  // namespace vmc
