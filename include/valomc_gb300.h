@@ -226,6 +226,42 @@ int vmc_server_poll(vmc_server *s, int64_t req_id, vmc_output *out, vmc_stats *s
 int vmc_server_wait(vmc_server *s, int64_t req_id, vmc_output *out, vmc_stats *stats, double timeout_s);
 int vmc_server_destroy(vmc_server *s);
 
+/* ---------------------------------------------------------------------------------- */
+/* Allocation-free run.  No counterpart in the reference.                               */
+/*                                                                                      */
+/* For callers that cannot let a library call cudaMalloc: hosts whose device memory is   */
+/* owned end to end by their own allocator (a framework's caching allocator, or a pool  */
+/* a serving process reserved up front), where a library-side cudaMalloc/cudaFree would */
+/* synchronise the device and take memory outside their accounting.  The caller passes  */
+/* the job's device arrays in buffers it owns (below) and receives host outputs; the    */
+/* kernel's scratch (launch control block, job table, event counters, emitting-face     */
+/* records) lives in one file-scope device array of VMC_NOALLOC_SCRATCH_BYTES that every */
+/* GPU which loads the library holds until the process exits.                           */
+/*                                                                                      */
+/* - The geometry comes from a resident mesh created beforehand (vmc_mesh_create).       */
+/* - One job per call, Philox streams only, at most VMC_NOALLOC_MAX_SOURCES emitting     */
+/*   faces; larger problems are refused with VMC_ERR_SIZE_LIMIT and a message.           */
+/* - The first call on a device looks up the scratch array's device address with that    */
+/*   device current; make that first call before any stream capture.                     */
+/* - Every call reuses the same scratch and clears what must start at zero; calls that   */
+/*   overlap on the GPU (other threads, other streams) race on it: serialise them.       */
+/* - It calls no cudaMalloc, cudaFree or other allocating device routine.                */
+#define VMC_NOALLOC_SCRATCH_BYTES (256 * 1024)
+#define VMC_NOALLOC_MAX_SOURCES 512
+
+typedef struct vmc_noalloc_buffers {
+  void *optics;     /* [Ne x 4] rows (mua, mus, g, n): float for VMC_FP32, double for VMC_FP64 */
+  uint8_t *bctype;  /* [Nb] boundary condition codes */
+  double *bcn;      /* [Nb] exterior refractive indices */
+  double *acc;      /* [2 Ne + 4 Nb] raw accumulators ER, EI, EBR, EBI, DEBR, DEBI */
+} vmc_noalloc_buffers;
+
+/* The job's optics / boundary arrays come from `job` (geometry pointers are ignored: the
+ * mesh is used), are copied into `dev`, and the normalised results are written to the
+ * host arrays of `out`, as vmc_run does. */
+int vmc_run_noalloc(vmc_mesh *mesh, const vmc_input *job, const vmc_options *opt, const vmc_noalloc_buffers *dev,
+                    vmc_output *out, vmc_stats *stats);
+
 /* Micro-benchmarks for the roofline denominators: random 32-byte-sector gathers over a
  * buffer of 'bytes' (dependent chains, like the element walk), and an FP64 FMA loop. */
 int vmc_bench_gather(int32_t device, int64_t bytes, double seconds, double *gbs_out);

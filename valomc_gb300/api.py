@@ -40,7 +40,7 @@ EXPORTS = [
     "vmc_abi_version", "vmc_status_string", "vmc_last_error", "vmc_default_options", "vmc_run",
     "vmc_build_neighbourhood", "vmc_mesh_create", "vmc_mesh_destroy", "vmc_mesh_device_bytes", "vmc_run_batch",
     "vmc_autotune", "vmc_server_create", "vmc_server_add_mesh", "vmc_server_submit", "vmc_server_poll",
-    "vmc_server_wait", "vmc_server_destroy", "vmc_bench_gather", "vmc_bench_fp64",
+    "vmc_server_wait", "vmc_server_destroy", "vmc_bench_gather", "vmc_bench_fp64", "vmc_run_noalloc",
 ]
 
 _p64 = C.POINTER(C.c_int64)
@@ -101,6 +101,11 @@ class VmcServerConfig(C.Structure):
     ]
 
 
+class VmcNoallocBuffers(C.Structure):
+    """Caller-owned device buffers of vmc_run_noalloc (device addresses as integers)."""
+    _fields_ = [("optics", C.c_void_p), ("bctype", C.c_void_p), ("bcn", C.c_void_p), ("acc", C.c_void_p)]
+
+
 class VmcError(RuntimeError):
     def __init__(self, status, where=""):
         self.status = status
@@ -148,6 +153,8 @@ def lib(build_if_missing=True):
         L.vmc_server_destroy.argtypes = [C.c_void_p]
         L.vmc_bench_gather.argtypes = [C.c_int32, C.c_int64, C.c_double, _pd]
         L.vmc_bench_fp64.argtypes = [C.c_int32, C.c_double, _pd]
+        L.vmc_run_noalloc.argtypes = [C.c_void_p, C.POINTER(VmcInput), C.POINTER(VmcOptions),
+                                      C.POINTER(VmcNoallocBuffers), C.POINTER(VmcOutput), C.POINTER(VmcStats)]
         _lib = L
     return _lib
 

@@ -19,7 +19,8 @@ LIB = os.path.join(BUILD, "libvalomc_gb300.so")
 INCLUDE = os.path.join(ROOT, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_UNITS = ["kern3d32.cu", "kern3d64.cu", "kern2d32.cu", "kern2d64.cu", "runtime.cu", "tools.cu", "server.cu"]
+CU_UNITS = ["kern3d32.cu", "kern3d64.cu", "kern2d32.cu", "kern2d64.cu", "runtime.cu", "tools.cu", "server.cu",
+            "noalloc.cu"]
 CPP_UNITS = ["host_setup.cpp"]
 APPS = {"MC3D": "app/mc3d_main.cpp", "MC2D": "app/mc2d_main.cpp"}
 
