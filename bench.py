@@ -258,9 +258,16 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--serve-seconds", type=float, default=6.0)
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--config", default="phantom", choices=["phantom", "fd", "batch", "serve"],
+                    help="phantom: the headline line; fd / batch / serve: the other workloads, one line each")
+    ap.add_argument("--batch-photon-scale", type=float, default=1.0)
+    ap.add_argument("--serve-rate", type=float, default=50.0)
+    ap.add_argument("--serve-window", type=float, default=10.0)
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
+    if args.config != "phantom":
+        return {"fd": bench_fd, "batch": bench_batch, "serve": bench_serve}[args.config](args)
 
     ws, rank, local = dist_env()
     dist = Dist(ws)
@@ -355,6 +362,117 @@ def main():
         out = line
         print(json.dumps(out), flush=True)
     dist.close()
+    return 0
+
+
+def bench_fd(args):
+    """The frequency-domain phantom (per-tet lognormal mua, U(8, 12) mus, 100 MHz): both forms."""
+    import valomc_gb300 as V
+    from valomc_gb300 import meshgen as mg
+    p = mg.config_3d_fd(nphoton=int(args.photons), seed=12345)
+    out = {"metric": "photons/s, frequency-domain phantom", "unit": "photons/s",
+           "config": {"workload": "FD phantom 648000 tets, f = 100 MHz, lognormal mua, U(8,12) mus"}}
+    for prec, name, n in ((V.VMC_FP32, "fp32", int(args.photons)), (V.VMC_FP64, "fp64", int(args.fp64_photons))):
+        mesh = V.Mesh(p, precision=prec)
+        q = p.copy(Nphoton=n)
+        V.run_batch([mesh], [q], precision=prec)
+        ks, st = [], None
+        for _ in range(max(1, args.steps)):
+            flush_l2()
+            _, st = V.run_batch([mesh], [q], precision=prec)
+            ks.append(st["seconds_kernel"])
+        k = float(np.median(ks))
+        out[name] = {"photons_per_s": n / k, "tet_steps_per_s": st["steps"] / k, "steps_per_photon": st["steps"] / n,
+                     "achieved_gbs_128B_per_step": 128 * st["steps"] / k / 1e9}
+        mesh.close()
+    out["value"] = out["fp32"]["photons_per_s"]
+    out["fp32_over_fp64"] = out["fp32"]["photons_per_s"] / out["fp64"]["photons_per_s"]
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def bench_batch(args):
+    """64 cubes (20-80 mm edges, 48k-3.07M tets each, ~46M in all) with their own optics and
+    pencil sources, photons log-uniform 1e5-1e7, in one persistent launch with the autotuned
+    launch shape, plain and through a CUDA graph."""
+    import valomc_gb300 as V
+    from valomc_gb300 import meshgen as mg
+    t0 = time.time()
+    probs = mg.config_batch(count=64, photon_scale=args.batch_photon_scale)
+    t_gen = time.time() - t0
+    t0 = time.time()
+    meshes = [V.Mesh(p) for p in probs]
+    t_mesh = time.time() - t0
+    tets = sum(p.Ne for p in probs)
+    photons = sum(p.Nphoton for p in probs)
+    t0 = time.time()
+    small = [p.copy(Nphoton=max(1, p.Nphoton // 50)) for p in probs]
+    tuned = V.autotune(meshes, small, budget_s=6.0)
+    t_tune = time.time() - t0
+    res = {}
+    for graph in (False, True):
+        o = V.options(block_size=tuned.block_size, blocks_per_sm=tuned.blocks_per_sm, fetch_chunk=tuned.fetch_chunk,
+                      use_graph=graph)
+        _, st = V.run_batch(meshes, probs, opts=o)
+        res["graph" if graph else "plain"] = {"kernel_s": st["seconds_kernel"], "wall_s": st["seconds_total"],
+                                              "photons_per_s": photons / st["seconds_kernel"],
+                                              "tet_steps_per_s": st["steps"] / st["seconds_kernel"],
+                                              "steps_per_photon": st["steps"] / photons}
+    dflt, st = V.run_batch(meshes, probs)
+    res["untuned_photons_per_s"] = photons / st["seconds_kernel"]
+    out = {"metric": "photons/s, 64 batched instances in one persistent launch", "unit": "photons/s",
+           "value": res["graph"]["photons_per_s"], "instances": len(probs), "tets": tets, "photons": photons,
+           "tuned": {"block_size": tuned.block_size, "blocks_per_sm": tuned.blocks_per_sm,
+                     "fetch_chunk": tuned.fetch_chunk, "tune_s": t_tune},
+           "mesh_gen_s": t_gen, "mesh_upload_s": t_mesh,
+           "device_mesh_bytes": int(sum(m.device_bytes for m in meshes)), **res,
+           "config": {"workload": "64 cubes L~logU[20,80] mm, pencil sources, config-4 optics",
+                      "photon_scale": args.batch_photon_scale}}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def bench_serve(args):
+    """Poisson request stream over 8 resident cubes (50k-2M tets), cosinic-disk or Gaussian
+    sources at random top points, config-4 optics, photons log-uniform 1e5-1e7."""
+    import valomc_gb300 as V
+    from valomc_gb300 import meshgen as mg
+    mix = mg.ServingMix(seed=5)
+    meshes = [V.Mesh(b) for b in mix.base]
+    srv = V.Server(max_slots=64, memory_budget=16 << 30)
+    ids = [srv.add_mesh(m) for m in meshes]
+    # warm the kernels and graphs
+    k, p = mix.request()
+    srv.wait(srv.submit(ids[k], p.copy(Nphoton=10000)))
+    rng = np.random.default_rng(55)
+    t0 = time.time()
+    t, sub = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / args.serve_rate)
+        if t > args.serve_window:
+            break
+        k, p = mix.request()
+        now = time.time() - t0
+        if t > now:
+            time.sleep(t - now)
+        sub.append((srv.submit(ids[k], p), p.Nphoton))
+    t_sub = time.time() - t0
+    lat, ph = [], 0
+    for rid, n in sub:
+        r = srv.wait(rid)
+        lat.append(r.stats["seconds_total"])
+        ph += n
+    wall = time.time() - t0
+    srv.close()
+    offered = sum(n for _, n in sub) / args.serve_window
+    out = {"metric": "serve p50/p99 latency and photons/s", "unit": "s", "rate_hz": args.serve_rate,
+           "window_s": args.serve_window, "requests": len(sub), "submit_s": t_sub, "drain_s": wall - t_sub,
+           "offered_photons_per_s": offered, "served_photons_per_s": ph / wall,
+           "stable": wall < 1.2 * args.serve_window + 2.0,
+           "p50_s": float(np.percentile(lat, 50)), "p90_s": float(np.percentile(lat, 90)),
+           "p99_s": float(np.percentile(lat, 99)), "value": float(np.percentile(lat, 99)),
+           "config": {"workload": "8 cubes 50k-2M tets, cosinic disk / gaussian sources, photons logU[1e5,1e7]"}}
+    print(json.dumps(out), flush=True)
     return 0
 
 

@@ -141,6 +141,10 @@ typedef struct vmc_options {
   /* photon index offset: this call simulates photons [photon_offset, photon_offset+Nphoton)
    * of the seed's stream (disjoint replicas, resumable runs) */
   int64_t photon_offset;
+  /* 1: record the launch (control-block reset + persistent kernel) as a CUDA graph and run
+   * the instantiated graph; repeated launches of the same shape update and reuse it */
+  int32_t use_graph;
+  int32_t reserved_opt;
 } vmc_options;
 
 typedef struct vmc_stats {
@@ -212,7 +216,7 @@ typedef struct vmc_server_config {
   int32_t device;
   int32_t precision;
   int32_t max_slots;          /* requests simulated concurrently */
-  int32_t reserved;
+  int32_t use_graph;          /* run each epoch's launches as an updated CUDA graph */
   int64_t memory_budget;      /* bytes of per-request device state admitted at once */
   int64_t epoch_photons;      /* photons per launch across all slots (latency/throughput knob) */
   int32_t block_size, blocks_per_sm;

@@ -38,6 +38,17 @@ def test_batch_equals_individual_runs(built, precision):
         np.testing.assert_allclose(r.EBR, one.EBR, rtol=RTOL, atol=1e-300)
 
 
+def test_batch_through_a_cuda_graph_equals_the_plain_launch(built):
+    jobs = small_jobs()
+    meshes = [V.Mesh(p) for p in jobs]
+    plain, _ = V.run_batch(meshes, jobs)
+    for _ in range(2):  # the second launch updates the instantiated graph in place
+        g, tot = V.run_batch(meshes, jobs, opts=V.options(use_graph=True))
+        assert tot["photons_done"] == sum(p.Nphoton for p in jobs)
+        for a, b in zip(plain, g):
+            np.testing.assert_allclose(b.ER, a.ER, rtol=RTOL, atol=1e-300)
+
+
 def test_autotuner_returns_a_valid_shape(built):
     jobs = small_jobs()
     meshes = [V.Mesh(p) for p in jobs]

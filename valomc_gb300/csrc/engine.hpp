@@ -61,6 +61,7 @@ int zero_job(JobBuffers &b, cudaStream_t st);
 struct LaunchSpec {
   int dim = 3, precision = VMC_FP32;
   bool fd = false, tape = false;
+  bool graph = false;  // launch through a (reused) CUDA graph
   int block = 0, blocks_per_sm = 0, chunk = 0;
   int64_t max_steps = 0;
 };

@@ -266,6 +266,29 @@ struct PinnedGuard {
     if (p) cudaFreeHost(p);
   }
 };
+
+// instantiated launch graphs of this thread, by kernel and launch shape
+struct GraphSlot {
+  const void *fn = nullptr;
+  int grid = 0, block = 0;
+  cudaGraphExec_t exec = nullptr;
+};
+GraphSlot &graph_slot(const void *fn, int grid, int block) {
+  static thread_local GraphSlot slots[16];
+  static thread_local int next_evict = 0;
+  for (auto &s : slots)
+    if (s.fn == fn && s.grid == grid && s.block == block) return s;
+  for (auto &s : slots)
+    if (!s.fn) {
+      s.fn = fn; s.grid = grid; s.block = block;
+      return s;
+    }
+  GraphSlot &s = slots[next_evict];
+  next_evict = (next_evict + 1) % 16;
+  if (s.exec) cudaGraphExecDestroy(s.exec);
+  s = GraphSlot{fn, grid, block, nullptr};
+  return s;
+}
 }  // namespace
 
 int launch_jobs(int device, const LaunchSpec &spec, const std::vector<JobDev> &jobs_in, const vmc_options *opt,
@@ -314,10 +337,47 @@ int launch_jobs(int device, const LaunchSpec &spec, const std::vector<JobDev> &j
   EventGuard e0, e1;
   VMC_CK(cudaEventCreate(&e0.e));
   VMC_CK(cudaEventCreate(&e1.e));
-  VMC_CK(cudaEventRecord(e0.e, st));
   void *args[] = {&lp};
-  VMC_CK(cudaLaunchKernel(fn, dim3(grid), dim3(block), args, 0, st));
-  VMC_CK(cudaEventRecord(e1.e, st));
+  StreamGuard gstream;
+  if (!spec.graph) {
+    VMC_CK(cudaEventRecord(e0.e, st));
+    VMC_CK(cudaLaunchKernel(fn, dim3(grid), dim3(block), args, 0, st));
+    VMC_CK(cudaEventRecord(e1.e, st));
+  } else {
+    // The control-block reset and the persistent kernel are recorded as a CUDA graph on a
+    // capture stream ordered after `st`; a graph of the same shape launched before on this
+    // thread is updated in place (cudaGraphExecUpdate) instead of instantiated again.
+    VMC_CK(cudaStreamCreateWithFlags(&gstream.s, cudaStreamNonBlocking));
+    VMC_CK(cudaEventRecord(e0.e, st));
+    VMC_CK(cudaStreamWaitEvent(gstream.s, e0.e, 0));
+    VMC_CK(cudaStreamBeginCapture(gstream.s, cudaStreamCaptureModeThreadLocal));
+    cudaError_t ce = cudaMemsetAsync(dctl.p, 0, sizeof(Ctl), gstream.s);
+    if (ce == cudaSuccess) ce = cudaLaunchKernel(fn, dim3(grid), dim3(block), args, 0, gstream.s);
+    cudaGraph_t graph = nullptr;
+    cudaError_t ee = cudaStreamEndCapture(gstream.s, &graph);
+    if (ce != cudaSuccess) { if (graph) cudaGraphDestroy(graph); return cuda_status(ce, "graph capture"); }
+    if (ee != cudaSuccess) return cuda_status(ee, "cudaStreamEndCapture");
+    GraphSlot &slot = graph_slot(fn, grid, block);
+    bool updated = false;
+    if (slot.exec) {
+      cudaGraphExecUpdateResultInfo info;
+      updated = cudaGraphExecUpdate(slot.exec, graph, &info) == cudaSuccess;
+      if (!updated) {
+        cudaGetLastError();
+        cudaGraphExecDestroy(slot.exec);
+        slot.exec = nullptr;
+      }
+    }
+    if (!updated) {
+      cudaError_t ie = cudaGraphInstantiate(&slot.exec, graph, 0);
+      if (ie != cudaSuccess) { cudaGraphDestroy(graph); slot.exec = nullptr; return cuda_status(ie, "cudaGraphInstantiate"); }
+    }
+    cudaGraphDestroy(graph);
+    VMC_CK(cudaEventRecord(e0.e, gstream.s));
+    VMC_CK(cudaGraphLaunch(slot.exec, gstream.s));
+    VMC_CK(cudaEventRecord(e1.e, gstream.s));
+    VMC_CK(cudaStreamWaitEvent(st, e1.e, 0));
+  }
 
   const bool poll = opt && (opt->progress || opt->cancel || opt->timeout_s > 0);
   int status = VMC_OK;
@@ -541,6 +601,7 @@ int vmc_run(const vmc_input *in, const vmc_options *opt_in, vmc_output *out, vmc
   spec.blocks_per_sm = o.blocks_per_sm;
   spec.chunk = o.fetch_chunk;
   spec.max_steps = o.max_steps;
+  spec.graph = o.use_graph != 0;
   LaunchResult lr;
   int ls = launch_jobs(o.device, spec, std::vector<JobDev>{d}, &o, stream, lr);
   if (ls != VMC_OK && ls != VMC_ERR_CANCELLED && ls != VMC_ERR_TIMEOUT) return ls;
@@ -652,6 +713,7 @@ int vmc_run_batch(vmc_mesh *const *meshes, const vmc_input *jobs, int32_t njobs,
     sp.blocks_per_sm = o.blocks_per_sm;
     sp.chunk = o.fetch_chunk;
     sp.max_steps = o.max_steps;
+    sp.graph = o.use_graph != 0;
     auto it = std::find_if(groups.begin(), groups.end(), [&](const Group &g) { return g.spec.dim == sp.dim && g.spec.fd == sp.fd; });
     if (it == groups.end()) { groups.push_back(Group{sp, {}}); it = groups.end() - 1; }
     it->idx.push_back(i);

@@ -140,6 +140,7 @@ void vmc_server::loop() {
       sp.fd = c.fd;
       sp.block = cfg.block_size;
       sp.blocks_per_sm = cfg.blocks_per_sm;
+      sp.graph = cfg.use_graph != 0;
       LaunchResult lr;
       int s = launch_jobs(cfg.device, sp, descs, nullptr, st, lr);
       for (size_t i = 0; i < c.rs.size(); i++) {

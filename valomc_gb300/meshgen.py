@@ -307,6 +307,55 @@ def config_batch(count=64, gen_seed=4, lmin=20, lmax=80, pmin=1e5, pmax=1e7, pho
     return out
 
 
+def cosinic_disk(r, BH, cx, cy, radius=1.0, z0=0.0):
+    """'c' (cosinic) on the top-face triangles whose centroid lies within ``radius`` of (cx, cy)."""
+    c = r[BH].mean(axis=1)
+    sel = top_face_mask(r, BH, z0) & (((c[:, 0] - cx) ** 2 + (c[:, 1] - cy) ** 2) <= radius * radius)
+    if not sel.any():  # at least the nearest top triangle
+        d = np.where(top_face_mask(r, BH, z0), (c[:, 0] - cx) ** 2 + (c[:, 1] - cy) ** 2, np.inf)
+        sel[np.argmin(d)] = True
+    return np.where(sel, ord("c"), ord("a")).astype(np.uint8)
+
+
+class ServingMix:
+    """The serving workload: 8 resident cubes with tet counts log-uniform in [50k, 2M]
+    (1 mm grid), requests choosing a mesh, a source (cosinic disk r = 1 mm, or a Gaussian
+    sigma = 1 mm direct footprint) at a uniform random top-face point, homogeneous optics as
+    in the batch workload, and photons log-uniform in [1e5, 1e7]."""
+
+    def __init__(self, seed=5, meshes=8, tmin=50_000, tmax=2_000_000, pmin=1e5, pmax=1e7):
+        self.rng = np.random.default_rng(seed)
+        self.pmin, self.pmax = pmin, pmax
+        self.base = []
+        for _ in range(meshes):
+            ntet = math.exp(self.rng.uniform(math.log(tmin), math.log(tmax)))
+            L = max(4, int(round((ntet / 6) ** (1 / 3))))
+            r, H, BH = box_mesh_3d(L, L, L)
+            ne, nb = len(H), len(BH)
+            self.base.append(Problem(dim=3, H=H, BH=BH, r=r, mua=np.full(ne, 0.01), mus=np.full(ne, 10.0),
+                                     g=np.full(ne, 0.9), n=np.full(ne, 1.4), BCType=np.full(nb, ord("a"), np.uint8),
+                                     BCn=np.ones(nb), Nphoton=1, seed=1))
+            self.base[-1].L = L
+
+    def request(self):
+        rng = self.rng
+        k = int(rng.integers(len(self.base)))
+        b = self.base[k]
+        L = b.L
+        cx, cy = rng.uniform(0.5, L - 0.5), rng.uniform(0.5, L - 0.5)
+        if rng.random() < 0.5:
+            bct, inten = cosinic_disk(b.r, b.BH, cx, cy), None
+        else:
+            bct, inten = gaussian_footprint(b.r, b.BH, cx, cy, sigma=1.0)
+        ne = b.Ne
+        p = Problem(dim=3, H=b.H, BH=b.BH, r=b.r, mua=np.full(ne, rng.uniform(0.005, 0.1)),
+                    mus=np.full(ne, rng.uniform(5, 20)), g=np.full(ne, rng.uniform(0.8, 0.95)),
+                    n=np.full(ne, rng.uniform(1.33, 1.45)), BCType=bct, BCn=np.ones(b.Nb), BCIntensity=inten,
+                    Nphoton=int(math.exp(rng.uniform(math.log(self.pmin), math.log(self.pmax)))),
+                    seed=int(rng.integers(1 << 31)))
+        return k, p
+
+
 # ---------------------------------------------------------------------------
 # text format of the external executables
 # ---------------------------------------------------------------------------
