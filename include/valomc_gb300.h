@@ -144,7 +144,10 @@ typedef struct vmc_options {
   /* 1: record the launch (control-block reset + persistent kernel) as a CUDA graph and run
    * the instantiated graph; repeated launches of the same shape update and reuse it */
   int32_t use_graph;
-  int32_t reserved_opt;
+  /* > 0: each CTA stages the element-fluence deposits of up to this many elements (rounded
+   * up to a power of 2, at most 4096) in shared memory and adds them to the FP64
+   * accumulator once at its end (FP32 tetrahedral walk, continuous wave, single job) */
+  int32_t stage_slots;
 } vmc_options;
 
 typedef struct vmc_stats {

@@ -49,6 +49,16 @@ def test_batch_through_a_cuda_graph_equals_the_plain_launch(built):
             np.testing.assert_allclose(b.ER, a.ER, rtol=RTOL, atol=1e-300)
 
 
+@pytest.mark.parametrize("slots", [64, 2048])
+def test_shared_memory_staging_equals_global_atomics(built, slots):
+    p = cases()["phantom3d"][0].copy(Nphoton=50000, seed=31)
+    mesh = V.Mesh(p)
+    plain, _ = V.run_batch([mesh], [p], opts=V.options(stage_slots=0))
+    staged, _ = V.run_batch([mesh], [p], opts=V.options(stage_slots=slots))
+    np.testing.assert_allclose(staged[0].ER, plain[0].ER, rtol=RTOL, atol=1e-300)
+    np.testing.assert_allclose(staged[0].EBR, plain[0].EBR, rtol=RTOL, atol=1e-300)
+
+
 def test_autotuner_returns_a_valid_shape(built):
     jobs = small_jobs()
     meshes = [V.Mesh(p) for p in jobs]

@@ -79,7 +79,7 @@ class VmcOptions(C.Structure):
         ("progress", PROGRESS_FN), ("progress_user", C.c_void_p), ("cancel", C.POINTER(C.c_int32)),
         ("tape", C.POINTER(C.c_uint32)), ("tape_off", _p64), ("tape_photons", C.c_int64),
         ("trace", _p64), ("trace_len", _p64), ("trace_stride", C.c_int64), ("trace_photons", C.c_int64),
-        ("photon_offset", C.c_int64), ("use_graph", C.c_int32), ("reserved_opt", C.c_int32),
+        ("photon_offset", C.c_int64), ("use_graph", C.c_int32), ("stage_slots", C.c_int32),
     ]
 
 
@@ -250,10 +250,13 @@ def _outputs(Ne, Nb, dim, want_hn):
 
 
 def options(precision=VMC_FP32, device=0, block_size=0, blocks_per_sm=0, fetch_chunk=0, max_steps=0,
-            timeout_s=0.0, stream_id=0, normalize=True, progress=None, cancel=None, photon_offset=0, use_graph=False):
+            timeout_s=0.0, stream_id=0, normalize=True, progress=None, cancel=None, photon_offset=0, use_graph=False,
+            stage_slots=None):
     o = VmcOptions()
     lib().vmc_default_options(C.byref(o))
     o.use_graph = int(bool(use_graph))
+    if stage_slots is not None:
+        o.stage_slots = int(stage_slots)
     o.precision, o.device = precision, device
     o.block_size, o.blocks_per_sm, o.fetch_chunk, o.max_steps = block_size, blocks_per_sm, fetch_chunk, max_steps
     o.timeout_s, o.stream_id, o.normalize, o.photon_offset = timeout_s, stream_id, int(bool(normalize)), photon_offset

@@ -62,6 +62,7 @@ struct LaunchSpec {
   int dim = 3, precision = VMC_FP32;
   bool fd = false, tape = false;
   bool graph = false;  // launch through a (reused) CUDA graph
+  int stage_slots = 0; // shared-memory staging slots per CTA (0: off)
   int block = 0, blocks_per_sm = 0, chunk = 0;
   int64_t max_steps = 0;
 };

@@ -33,9 +33,24 @@ __device__ __forceinline__ int find_job(const LaunchParams &lp, int64_t p) {
 
 template <class W, class R>
 __global__ void __launch_bounds__(256, W::kMinBlocks) pool_kernel(const LaunchParams lp) {
+  extern __shared__ __align__(16) unsigned char vmc_smem[];
   W s;
   R rng;
   const JobDev *J = lp.jobs;
+  Stage stg{nullptr, nullptr, 0u};
+  if constexpr (W::kStaged) {
+    if (lp.stage_slots > 0) {
+      stg.val = reinterpret_cast<double *>(vmc_smem);
+      stg.tag = reinterpret_cast<int32_t *>(vmc_smem + sizeof(double) * lp.stage_slots);
+      stg.mask = (uint32_t)lp.stage_slots - 1u;
+      for (int i = threadIdx.x; i < lp.stage_slots; i += blockDim.x) {
+        stg.tag[i] = -1;
+        stg.val[i] = 0.0;
+      }
+      __syncthreads();
+    }
+  }
+  s.stage = stg;
   bool alive = false, done = false;
   uint32_t n_steps = 0, n_scat = 0, n_done = 0;
   long long chunk_next = 0, chunk_end = 0;
@@ -81,6 +96,17 @@ __global__ void __launch_bounds__(256, W::kMinBlocks) pool_kernel(const LaunchPa
         if (r == kDied) n_steps++;
         alive = false;
         n_done++;
+      }
+    }
+  }
+  if constexpr (W::kStaged) {
+    // every warp of the CTA has left the loop: add the staged sums to the accumulator
+    if (lp.stage_slots > 0) {
+      __syncthreads();
+      double *ER = lp.jobs[0].ER;
+      for (int i = threadIdx.x; i < lp.stage_slots; i += blockDim.x) {
+        const int32_t t = stg.tag[i];
+        if (t >= 0 && stg.val[i] != 0.0) atomicAdd(ER + t, stg.val[i]);
       }
     }
   }

@@ -308,7 +308,14 @@ int launch_jobs(int device, const LaunchSpec &spec, const std::vector<JobDev> &j
   int block = spec.block > 0 ? spec.block : 256;
   if (block % 32 || block > 256) { set_error("block size must be a multiple of 32, at most 256"); return VMC_ERR_INVALID_ARGUMENT; }
   int per_sm = 0;
-  VMC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, 0));
+  // shared-memory staging of deposits: FP32 tetrahedral walk, continuous wave, one job
+  int stage_slots = 0;
+  if (spec.stage_slots > 0 && spec.dim == 3 && spec.precision == VMC_FP32 && !spec.fd && jobs.size() == 1) {
+    stage_slots = 1;
+    while (stage_slots < spec.stage_slots && stage_slots < 4096) stage_slots <<= 1;
+  }
+  const size_t smem = (size_t)stage_slots * (sizeof(double) + sizeof(int32_t));
+  VMC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, smem));
   if (per_sm < 1) { set_error("kernel does not fit on an SM at this block size"); return VMC_ERR_INVALID_ARGUMENT; }
   if (spec.blocks_per_sm > 0) per_sm = std::min(per_sm, spec.blocks_per_sm);
   const int grid = per_sm * sms;
@@ -334,6 +341,8 @@ int launch_jobs(int device, const LaunchSpec &spec, const std::vector<JobDev> &j
   lp.total = total;
   lp.max_steps = spec.max_steps > 0 ? spec.max_steps : 10000000;
   lp.ctl = dctl.p;
+  lp.stage_slots = stage_slots;
+  lp.pad = 0;
   EventGuard e0, e1;
   VMC_CK(cudaEventCreate(&e0.e));
   VMC_CK(cudaEventCreate(&e1.e));
@@ -341,7 +350,7 @@ int launch_jobs(int device, const LaunchSpec &spec, const std::vector<JobDev> &j
   StreamGuard gstream;
   if (!spec.graph) {
     VMC_CK(cudaEventRecord(e0.e, st));
-    VMC_CK(cudaLaunchKernel(fn, dim3(grid), dim3(block), args, 0, st));
+    VMC_CK(cudaLaunchKernel(fn, dim3(grid), dim3(block), args, smem, st));
     VMC_CK(cudaEventRecord(e1.e, st));
   } else {
     // The control-block reset and the persistent kernel are recorded as a CUDA graph on a
@@ -352,7 +361,7 @@ int launch_jobs(int device, const LaunchSpec &spec, const std::vector<JobDev> &j
     VMC_CK(cudaStreamWaitEvent(gstream.s, e0.e, 0));
     VMC_CK(cudaStreamBeginCapture(gstream.s, cudaStreamCaptureModeThreadLocal));
     cudaError_t ce = cudaMemsetAsync(dctl.p, 0, sizeof(Ctl), gstream.s);
-    if (ce == cudaSuccess) ce = cudaLaunchKernel(fn, dim3(grid), dim3(block), args, 0, gstream.s);
+    if (ce == cudaSuccess) ce = cudaLaunchKernel(fn, dim3(grid), dim3(block), args, smem, gstream.s);
     cudaGraph_t graph = nullptr;
     cudaError_t ee = cudaStreamEndCapture(gstream.s, &graph);
     if (ce != cudaSuccess) { if (graph) cudaGraphDestroy(graph); return cuda_status(ce, "graph capture"); }
@@ -602,6 +611,7 @@ int vmc_run(const vmc_input *in, const vmc_options *opt_in, vmc_output *out, vmc
   spec.chunk = o.fetch_chunk;
   spec.max_steps = o.max_steps;
   spec.graph = o.use_graph != 0;
+  spec.stage_slots = o.stage_slots;
   LaunchResult lr;
   int ls = launch_jobs(o.device, spec, std::vector<JobDev>{d}, &o, stream, lr);
   if (ls != VMC_OK && ls != VMC_ERR_CANCELLED && ls != VMC_ERR_TIMEOUT) return ls;
@@ -714,6 +724,7 @@ int vmc_run_batch(vmc_mesh *const *meshes, const vmc_input *jobs, int32_t njobs,
     sp.chunk = o.fetch_chunk;
     sp.max_steps = o.max_steps;
     sp.graph = o.use_graph != 0;
+    sp.stage_slots = o.stage_slots;
     auto it = std::find_if(groups.begin(), groups.end(), [&](const Group &g) { return g.spec.dim == sp.dim && g.spec.fd == sp.fd; });
     if (it == groups.end()) { groups.push_back(Group{sp, {}}); it = groups.end() - 1; }
     it->idx.push_back(i);

@@ -139,6 +139,18 @@ struct LaunchParams {
   int64_t total;              // sum of photon counts
   int64_t max_steps;
   Ctl *ctl;
+  int32_t stage_slots;        // > 0: per-CTA shared-memory staging of ER deposits (power of 2)
+  int32_t pad;
+};
+
+// Shared-memory staging of element deposits: a direct-mapped table of stage_slots entries
+// per CTA (element tag, FP64 sum).  A flush into an element whose slot this CTA holds is a
+// shared-memory add; a free slot is claimed by the first element hashed to it; anything else
+// goes to the global atomic.  The table is added to global memory once, when the CTA ends.
+struct Stage {
+  int32_t *tag;
+  double *val;
+  uint32_t mask;  // slots - 1; 0 disables staging
 };
 
 }  // namespace vmc

@@ -25,6 +25,8 @@ __device__ __forceinline__ bool ray_seg(const double R[2], const double D[2], co
 template <bool FD, class R>
 struct Walk2D64 {
   static constexpr int kMinBlocks = 1;
+  static constexpr bool kStaged = false;
+  Stage stage;
   using Tr = typename TraceFor<R>::type;
   double pos[2], dir[2];
   double w, prop, phase, cph, sph;
@@ -245,6 +247,8 @@ struct Walk2D64 {
 template <bool FD, class R>
 struct Walk2D32 {
   static constexpr int kMinBlocks = 4;
+  static constexpr bool kStaged = false;
+  Stage stage;
   using Tr = typename TraceFor<R>::type;
   float px, py, dx, dy;
   float w, prop, phase;
@@ -277,7 +281,7 @@ struct Walk2D32 {
     phase = (float)J.phase0;
     float4 o = optics(J, el);
     mua = o.x; mus = o.y; g = o.z; nidx = o.w;
-    prop = __fdividef(-logf(unif_open_f(rng)), mus);
+    prop = free_path_f(unif_open_f(rng), mus);
     acc = accI = 0.0f;
     nsteps = 0;
   }
@@ -388,7 +392,7 @@ struct Walk2D32 {
     const float x = mua * ds;
     if (!FD) {
       if (mua > 0.0f) {
-        float dep = -w * expm1f(-x);
+        float dep = w * one_minus_exp_neg(x);
         acc += dep;
         w -= dep;
       } else {
@@ -412,7 +416,7 @@ struct Walk2D32 {
     if (prop <= 0.0f) {
       int res = kAlive;
       if (mus > 0.0f) { scatter(rng); res = kScattered; }
-      prop = __fdividef(-logf(unif_open_f(rng)), mus);
+      prop = free_path_f(unif_open_f(rng), mus);
       return res;
     }
     const float nx = lsel(l0, l1, l2, nf, 0), ny = lsel(l0, l1, l2, nf, 1);
@@ -450,7 +454,7 @@ struct Walk2D32 {
     }
     const float4 o2 = optics(J, nextel);
     if (mus <= 0.0f && o2.y > 0.0f) {
-      prop = __fdividef(-logf(unif_open_f(rng)), o2.y);
+      prop = free_path_f(unif_open_f(rng), o2.y);
       if (roulette(J, rng)) return die(J, kEvRoulette);
       if (nidx != o2.w && fresnel(rng, nx, ny, nidx / o2.w, false)) return kAlive;
     } else {

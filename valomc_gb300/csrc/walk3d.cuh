@@ -79,12 +79,30 @@ __device__ __forceinline__ bool fresnel_reflects_f(R &rng, float eta, float ci, 
 
 __device__ __forceinline__ bool is_mirror(uint8_t bt) { return bt == 'm' || bt == 'L' || bt == 'I' || bt == 'C'; }
 
+// 1 - exp(-x) for x >= 0 in FP32 without cancellation: below 0.1 the series to x^5
+// (truncation x^6/720, relative x^5/720 < 1.4e-8); above, 1 - exp(-x) from the fast
+// exponential (relative error < 2^-22 / (1 - e^-0.1) ~ 1.3e-6 at the cut, falling beyond).
+__device__ __forceinline__ float one_minus_exp_neg(float x) {
+  if (x < 0.1f)
+    return x * (1.0f + x * (-0.5f + x * (1.0f / 6.0f + x * (-1.0f / 24.0f + x * (1.0f / 120.0f)))));
+  return 1.0f - __expf(-x);
+}
+
+// distance to the next interaction, -log(U) / mus, with U in (0, 1).  The fast logarithm's
+// absolute error (~1e-7) can make -log(U) of a U within 1e-7 of 1 come out at or just
+// below zero; such a draw is an interaction at once, as it nearly is exactly.
+__device__ __forceinline__ float free_path_f(float u, float mus) {
+  return __fdividef(fmaxf(-__logf(u), 0.0f), mus);
+}
+
 // =====================================================================================
 // plain FP64 form
 // =====================================================================================
 template <bool FD, class R>
 struct Walk3D64 {
   static constexpr int kMinBlocks = 1;  // ~125 registers: 2 CTAs of 256 per SM
+  static constexpr bool kStaged = false;
+  Stage stage;
   using Tr = typename TraceFor<R>::type;
   double pos[3], dir[3];
   double w, prop, phase, cph, sph;
@@ -331,6 +349,7 @@ struct Walk3D32 {
   // 4 CTAs of 256 per SM (64 registers): the walk is latency bound and more resident
   // warps beat the few spills (measured +7% over 3 CTAs on the 648k-tet phantom)
   static constexpr int kMinBlocks = 4;
+  static constexpr bool kStaged = !FD;
   using Tr = typename TraceFor<R>::type;
   float px, py, pz, dx, dy, dz;
   float w, prop, phase;
@@ -339,6 +358,7 @@ struct Walk3D32 {
   int el;
   int32_t nsteps;
   bool outward;  // launched out through its own entry face
+  Stage stage;   // shared-memory staging of ER deposits (continuous wave, single job)
   Tr tr;
 
   __device__ __forceinline__ float4 optics(const JobDev &J, int e) const {
@@ -364,13 +384,14 @@ struct Walk3D32 {
     phase = (float)J.phase0;
     float4 o = optics(J, el);
     mua = o.x; mus = o.y; g = o.z; nidx = o.w;
-    prop = __fdividef(-logf(unif_open_f(rng)), mus);
+    prop = free_path_f(unif_open_f(rng), mus);
     acc = accI = 0.0f;
     nsteps = 0;
   }
 
   __device__ __forceinline__ void flush(const JobDev &J) {
-    add_f(J.ER + el, acc);
+    if (!FD) add_staged(stage, J.ER, el, acc);
+    else add_f(J.ER + el, acc);
     if (FD) add_f(J.EI + el, accI);
     acc = accI = 0.0f;
   }
@@ -398,17 +419,20 @@ struct Walk3D32 {
       ct = 2.0f * xi - 1.0f;
     }
     ct = fminf(1.0f, fmaxf(-1.0f, ct));
-    float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+    const float s2 = fmaxf(0.0f, 1.0f - ct * ct);
+    const float st = s2 > 0.0f ? s2 * rsqrtf(s2) : 0.0f;
     float sp, cp;
-    sincospif(2.0f * unif_closed_f(rng), &sp, &cp);
+    // phi uniform on [-pi, pi] (the reference's [0, 2 pi] shifted; same distribution)
+    __sincosf((float)kPi * (2.0f * unif_closed_f(rng) - 1.0f), &sp, &cp);
     float nx, ny, nz;
     if (fabsf(dz) > 0.999f) {
       nx = st * cp;
       ny = st * sp;
       nz = copysignf(ct, dz);
     } else {
-      float sq = sqrtf(1.0f - dz * dz);
-      float isq = 1.0f / sq;
+      const float s2z = 1.0f - dz * dz;
+      const float isq = rsqrtf(s2z);
+      const float sq = s2z * isq;
       nx = st * (dx * dz * cp - dy * sp) * isq + dx * ct;
       ny = st * (dy * dz * cp + dx * sp) * isq + dy * ct;
       nz = -st * cp * sq + dz * ct;
@@ -488,7 +512,7 @@ struct Walk3D32 {
     const float x = mua * ds;
     if (!FD) {
       if (mua > 0.0f) {
-        float dep = -w * expm1f(-x);
+        float dep = w * one_minus_exp_neg(x);
         acc += dep;
         w -= dep;
       } else {
@@ -514,7 +538,7 @@ struct Walk3D32 {
     if (prop <= 0.0f) {
       int res = kAlive;
       if (mus > 0.0f) { scatter(rng); res = kScattered; }
-      prop = __fdividef(-logf(unif_open_f(rng)), mus);
+      prop = free_path_f(unif_open_f(rng), mus);
       return res;
     }
     const float4 pf = nf == 0 ? p0 : nf == 1 ? p1 : nf == 2 ? p2 : p3;
@@ -547,7 +571,7 @@ struct Walk3D32 {
     }
     const float4 o2 = optics(J, nextel);
     if (mus <= 0.0f && o2.y > 0.0f) {
-      prop = __fdividef(-logf(unif_open_f(rng)), o2.y);
+      prop = free_path_f(unif_open_f(rng), o2.y);
       if (roulette(J, rng)) return die(J, kEvRoulette);
       if (nidx != o2.w && fresnel(rng, pf.x, pf.y, pf.z, nidx / o2.w)) return kAlive;
     } else {

@@ -174,6 +174,23 @@ __device__ __forceinline__ void add_f(double *p, float v) {
   if (v != 0.0f) atomicAdd(p, f2d_int(v));
 }
 
+// element deposit through the CTA's shared-memory stage when it holds (or can claim) the
+// element's slot, else straight to the global accumulator
+__device__ __forceinline__ void add_staged(const Stage &S, double *ER, int el, float v) {
+  if (v == 0.0f) return;
+  const double d = f2d_int(v);
+  if (S.mask) {
+    const uint32_t h = (((uint32_t)el * 2654435761u) >> 16) & S.mask;  // Fibonacci hash, high bits
+    int32_t t = S.tag[h];
+    if (t < 0) t = atomicCAS(S.tag + h, -1, el), t = (t < 0) ? el : t;
+    if (t == el) {
+      atomicAdd(S.val + h, d);
+      return;
+    }
+  }
+  atomicAdd(ER + el, d);
+}
+
 // ---- FP32 launch for the tracking form: same draws and sampling laws as CreatePhoton,
 // evaluated in float from the FP32 face records (cos(asin(s)) = sqrt(1 - s^2)) ----
 __device__ __forceinline__ int pick_source_f(const JobDev &J, float xi) {
