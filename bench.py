@@ -1,7 +1,7 @@
 """Benchmark of the photon-propagation path on the 60x60x30 mm inclusion phantom
 (648 000 tetrahedra, 1 mm grid, Gaussian sigma = 1 mm direct source, Fresnel boundary).
 
-A step is one simulation of ``--photons`` photons (default 1e7) through the FP32 tracking
+A step is one simulation of ``--photons`` photons (default 1e8) through the FP32 tracking
 form with the mesh resident on the device.  Reported:
   value       photons/s with the mesh and job resident (whole-job: setup of the job,
               kernel, read-back), max over ranks
@@ -162,7 +162,7 @@ def ncu_traffic():
     return None
 
 
-def cpu_baseline(p, seconds_target=12.0, threads=None):
+def cpu_baseline(p, seconds_target=12.0, threads=None, name="phantom"):
     """The CPU oracle on all host cores, on a sample sized to ~seconds_target of work."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
@@ -175,7 +175,7 @@ def cpu_baseline(p, seconds_target=12.0, threads=None):
     r = oracle.run(p, rng=oracle.RNG_MT, nthreads=threads, nphoton=n, normalize=False)
     rate = n / r.seconds
     return {"value": rate, "unit": "photons/s", "cores": threads, "kind": "port",
-            "sample": f"{n} photons of the phantom workload (MT19937, {threads} OpenMP threads), "
+            "sample": f"{n} photons of the {name} workload (MT19937, {threads} OpenMP threads), "
                       f"{r.seconds:.1f} s", "steps_per_photon": r.steps / n}
 
 
@@ -252,13 +252,13 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--photons", type=float, default=1e7)
-    ap.add_argument("--fp64-photons", type=float, default=1e6)
+    ap.add_argument("--photons", type=float, default=1e8)
+    ap.add_argument("--fp64-photons", type=float, default=1e7)
     ap.add_argument("--ref-seconds", type=float, default=10.0)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--serve-seconds", type=float, default=6.0)
     ap.add_argument("--no-extras", action="store_true")
-    ap.add_argument("--config", default="phantom", choices=["phantom", "fd", "batch", "serve"],
+    ap.add_argument("--config", default="phantom", choices=["phantom", "fd", "batch", "serve", "square2d"],
                     help="phantom: the headline line; fd / batch / serve: the other workloads, one line each")
     ap.add_argument("--batch-photon-scale", type=float, default=1.0)
     ap.add_argument("--serve-rate", type=float, default=50.0)
@@ -267,7 +267,7 @@ def main():
     if args.impl == "reference":
         return reference_arm(args)
     if args.config != "phantom":
-        return {"fd": bench_fd, "batch": bench_batch, "serve": bench_serve}[args.config](args)
+        return {"fd": bench_fd, "batch": bench_batch, "serve": bench_serve, "square2d": bench_square2d}[args.config](args)
 
     ws, rank, local = dist_env()
     dist = Dist(ws)
@@ -348,7 +348,7 @@ def main():
             line["roofline"]["l2_gather_frac"] = achieved / gather
             # plain FP64 form on the same mesh
             n64 = int(args.fp64_photons)
-            r64 = V.run(p, precision=V.VMC_FP64, device=dev, nphoton=n64)
+            V.run(p, precision=V.VMC_FP64, device=dev, nphoton=min(n64, 1_000_000))  # warm-up
             r64b = V.run(p, precision=V.VMC_FP64, device=dev, nphoton=n64, seed=777)
             fp64_rate = n64 / r64b.stats["seconds_kernel"]
             fp32_rate = nph / kmean
@@ -387,6 +387,27 @@ def bench_fd(args):
         mesh.close()
     out["value"] = out["fp32"]["photons_per_s"]
     out["fp32_over_fp64"] = out["fp32"]["photons_per_s"] / out["fp64"]["photons_per_s"]
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def bench_square2d(args):
+    """The 2D square (10x10 mm, 200 triangles, cosinic source on edges 4..7, 1e6 photons):
+    both forms through vmc_run (host buffers), and the CPU oracle on all host cores."""
+    import valomc_gb300 as V
+    from valomc_gb300 import meshgen as mg
+    p = mg.config_2d_square(nphoton=1_000_000, seed=12345)
+    out = {"metric": "photons/s, 2D square", "unit": "photons/s",
+           "config": {"workload": "10x10 mm square, 200 triangles, cosinic edges 4-7, 1e6 photons"}}
+    for prec, name in ((V.VMC_FP64, "fp64"), (V.VMC_FP32, "fp32")):
+        V.run(p, precision=prec)
+        rs = [V.run(p, precision=prec) for _ in range(max(1, args.steps))]
+        k = min(r.stats["seconds_kernel"] for r in rs)
+        tot = min(r.stats["seconds_total"] for r in rs)
+        out[name] = {"photons_per_s_kernel": p.Nphoton / k, "photons_per_s_e2e": p.Nphoton / tot,
+                     "steps_per_photon": rs[0].stats["steps"] / p.Nphoton}
+    out["cpu_baseline"] = cpu_baseline(p, seconds_target=5.0, name="2D square")
+    out["value"] = out["fp64"]["photons_per_s_e2e"]
     print(json.dumps(out), flush=True)
     return 0
 

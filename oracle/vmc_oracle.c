@@ -160,6 +160,14 @@ static uint32_t u_word(urng *u) {
   }
 }
 
+/* Philox streams only: the end of a free path (a scatter event) starts a new counter
+   block and drops the words left in the current one, so that the draws of one event come
+   from one block (the GPU kernels compute that block for all scattering lanes at once).
+   The reference's MT19937 stream and a tape are consumed word by word. */
+static void u_align(urng *u) {
+  if (u->kind == VO_RNG_PHILOX) u->ph.nbuf = 0;
+}
+
 /* the four mappings of cpp/3d/mt_rng.hpp:187-204 */
 static double UnifClosed(urng *u) { return (double)u_word(u) * (1.0 / 4294967295.0); }
 static double UnifOpen(urng *u) { return ((double)u_word(u) + 0.5) * (1.0 / 4294967296.0); }
@@ -803,7 +811,7 @@ static void propagate3(const engine *E, worker *w, photon *ph, int64_t max_steps
       for (int c = 0; c < 3; c++) ph->pos[c] += ph->dir[c] * ds;
       score_step(E, w, ph, ds);
       prop -= ds;
-      if (prop <= 0.0) break;
+      if (prop <= 0.0) { u_align(&w->u); break; }
       if (ph->nextel < 0) {
         ib = -1 - ph->nextel;
         char bt = P->BCType[ib];
@@ -1027,7 +1035,7 @@ static void propagate2(const engine *E, worker *w, photon *ph, int64_t max_steps
       ph->pos[1] += ph->dir[1] * ds;
       score_step(E, w, ph, ds);
       prop -= ds;
-      if (prop <= 0.0) break;
+      if (prop <= 0.0) { u_align(&w->u); break; }
       if (ph->nextel < 0) {
         ib = -1 - ph->nextel;
         char bt = P->BCType[ib];

@@ -2,7 +2,8 @@
 //
 // PhiloxRng: Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy
 // as 1, 2, 3", SC'11), one counter stream per photon: key = seed, counter = (photon lo,
-// photon hi, block, stream).  Words are consumed in order x, y, z, w of each block.
+// photon hi, block, stream).  Words are consumed in order x, y, z, w of each block, except
+// that each scatter event (the end of a free path) starts a new block (align()).
 // TapeRng: a caller-supplied word sequence (trajectory replay).
 // The double mappings are the reference's (cpp/3d/mt_rng.hpp:187-204); the float mappings
 // keep 24 (closed, half-open) or 23 (open) bits so every value is exact in FP32.
@@ -11,18 +12,27 @@
 
 namespace vmc {
 
+// The per-photon constants of the counter (key, photon index high word, stream) wait in a
+// shared-memory slot of the lane, read once per block, so that only the words that change
+// occupy registers.  A pool kernel runs at most 256 threads per CTA.
+__device__ __forceinline__ uint4 *philox_slot() {
+  __shared__ uint4 slots[256];
+  return slots + threadIdx.x;
+}
+
 struct PhiloxRng {
-  uint32_t k0, k1, c0, c1, c2, c3;
+  uint32_t c0, c2;  // photon index low word, block counter
   uint4 buf;
   int32_t n;
 
   __device__ __forceinline__ void start(uint64_t seed, uint32_t stream, uint64_t photon) {
-    k0 = (uint32_t)seed; k1 = (uint32_t)(seed >> 32);
-    c0 = (uint32_t)photon; c1 = (uint32_t)(photon >> 32);
-    c2 = 0; c3 = stream; n = 0;
+    *philox_slot() = make_uint4((uint32_t)seed, (uint32_t)(seed >> 32), (uint32_t)(photon >> 32), stream);
+    c0 = (uint32_t)photon;
+    c2 = 0; n = 0;
   }
   __device__ __forceinline__ void block() {
-    uint32_t x0 = c0, x1 = c1, x2 = c2, x3 = c3, a = k0, b = k1;
+    const uint4 k = *philox_slot();
+    uint32_t x0 = c0, x1 = k.z, x2 = c2, x3 = k.w, a = k.x, b = k.y;
 #pragma unroll
     for (int r = 0; r < 10; r++) {
       if (r) { a += 0x9E3779B9u; b += 0xBB67AE85u; }
@@ -43,6 +53,11 @@ struct PhiloxRng {
     return r;
   }
   __device__ __forceinline__ bool exhausted() const { return false; }
+  // A scatter event starts a fresh block: its draws (direction, then the next free path;
+  // at most 3 words) come from one block that every scattering lane of a warp computes
+  // together, instead of each lane computing blocks at a different draw.  Words left in
+  // the previous block are dropped.
+  __device__ __forceinline__ void align() { n = 0; }
 };
 
 struct TapeRng {
@@ -55,6 +70,7 @@ struct TapeRng {
     return 0x80000000u;
   }
   __device__ __forceinline__ bool exhausted() const { return out; }
+  __device__ __forceinline__ void align() {}  // a tape is consumed word by word
 };
 
 // reference mappings (double)

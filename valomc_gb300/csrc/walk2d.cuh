@@ -169,6 +169,7 @@ struct Walk2D64 {
     prop -= ds;
     if (prop <= 0.0) {
       int res = kAlive;
+      rng.align();
       if (mus > 0.0) { scatter(rng); res = kScattered; }
       prop = -log(unif_open(rng)) / mus;
       return res;
@@ -228,7 +229,7 @@ struct Walk2D64 {
         edge_normal(V, nf, nor);
         if (fresnel(rng, nor, nidx / n2, nf, false)) return kAlive;
       }
-      prop *= mus / mus2;
+      if (mus2 != mus) prop *= mus / mus2;  // x (mus / mus) == x: skip the division
     }
     const int4 nb2 = __ldg(reinterpret_cast<const int4 *>((reinterpret_cast<const Tri64 *>(J.geom) + nextel)->nbr));
     int f2 = nb2.x == el ? 0 : nb2.y == el ? 1 : nb2.z == el ? 2 : -1;
@@ -415,6 +416,7 @@ struct Walk2D32 {
     prop -= ds;
     if (prop <= 0.0f) {
       int res = kAlive;
+      rng.align();
       if (mus > 0.0f) { scatter(rng); res = kScattered; }
       prop = free_path_f(unif_open_f(rng), mus);
       return res;
@@ -460,7 +462,7 @@ struct Walk2D32 {
     } else {
       if (roulette(J, rng)) return die(J, kEvRoulette);
       if (nidx != o2.w && fresnel(rng, nx, ny, nidx / o2.w, false)) return kAlive;
-      prop *= mus / o2.y;
+      if (o2.y != mus) prop *= mus / o2.y;
     }
     flush(J);
     el = nextel;

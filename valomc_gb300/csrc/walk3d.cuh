@@ -249,6 +249,7 @@ struct Walk3D64 {
     prop -= ds;
     if (prop <= 0.0) {
       int res = kAlive;
+      rng.align();
       if (mus > 0.0) { scatter(J, rng); res = kScattered; }
       prop = -log(unif_open(rng)) / mus;
       return res;
@@ -312,7 +313,7 @@ struct Walk3D64 {
         face_normal(V, nf, nor);
         if (fresnel(rng, nor, nidx / n2, nf)) return kAlive;
       }
-      prop *= mus / mus2;
+      if (mus2 != mus) prop *= mus / mus2;  // x (mus / mus) == x: skip the division
     }
     // reverse-face lookup, MC3D.hpp:1616-1628
     const int4 nb2 = __ldg(reinterpret_cast<const int4 *>((reinterpret_cast<const Tet64 *>(J.geom) + nextel)->nbr));
@@ -537,6 +538,7 @@ struct Walk3D32 {
     prop -= ds;
     if (prop <= 0.0f) {
       int res = kAlive;
+      rng.align();
       if (mus > 0.0f) { scatter(rng); res = kScattered; }
       prop = free_path_f(unif_open_f(rng), mus);
       return res;
@@ -577,7 +579,7 @@ struct Walk3D32 {
     } else {
       if (roulette(J, rng)) return die(J, kEvRoulette);
       if (nidx != o2.w && fresnel(rng, pf.x, pf.y, pf.z, nidx / o2.w)) return kAlive;
-      prop *= mus / o2.y;
+      if (o2.y != mus) prop *= mus / o2.y;
     }
     flush(J);
     el = nextel;
