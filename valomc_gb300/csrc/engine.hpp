@@ -80,10 +80,12 @@ int launch_jobs(int device, const LaunchSpec &spec, const std::vector<JobDev> &j
 int collect_job(const HostJob &j, const DeviceMesh &m, const JobBuffers &b, int64_t nphoton, bool normalize,
                 vmc_output *out, vmc_stats *st, cudaStream_t stream);
 
-const void *kernel_3d64(bool fd, bool tape);
-const void *kernel_3d32(bool fd, bool tape);
-const void *kernel_2d64(bool fd, bool tape);
-const void *kernel_2d32(bool fd, bool tape);
-const void *select_kernel(const LaunchSpec &s);
+const void *kernel_3d64(bool fd, bool tape, bool one);
+const void *kernel_3d32(bool fd, bool tape, bool one);
+const void *kernel_2d64(bool fd, bool tape, bool one);
+const void *kernel_2d32(bool fd, bool tape, bool one);
+// one: the single-job form (descriptor and round keys in LaunchParams::job0 / rk)
+const void *select_kernel(const LaunchSpec &s, bool one = false);
+void set_single_job(LaunchParams &lp, const JobDev &job);
 
 }  // namespace vmc

@@ -1,11 +1,11 @@
-// kern3d64.cu -- instantiations of the photon-pool kernel for the Walk3D64 walker
-// (continuous-wave / frequency-domain x Philox / replay tape).  A separate translation unit
-// per walker so the build compiles them in parallel.
+// kern3d64.cu -- instantiations of the photon-pool kernel for the Walk3D64 walker:
+// continuous-wave / frequency-domain x (Philox, replay tape).  A separate translation
+// unit per walker so the build compiles them in parallel.
 #include "pool.cuh"
 
 namespace vmc {
 
-const void *kernel_3d64(bool fd, bool tape) {
+const void *kernel_3d64(bool fd, bool tape, bool /*one: FP32 walks only*/) {
   if (fd) {
     if (tape) return reinterpret_cast<const void *>(&pool_kernel<Walk3D64<true, TapeRng>, TapeRng>);
     return reinterpret_cast<const void *>(&pool_kernel<Walk3D64<true, PhiloxRng>, PhiloxRng>);

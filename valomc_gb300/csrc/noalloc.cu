@@ -192,7 +192,7 @@ extern "C" int vmc_run_noalloc(vmc_mesh *mesh, const vmc_input *job, const vmc_o
   VMC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, 0));
   if (o.blocks_per_sm > 0) per_sm = std::min(per_sm, (int)o.blocks_per_sm);
   if (per_sm < 1) return VMC_ERR_INVALID_ARGUMENT;
-  LaunchParams lp;
+  LaunchParams lp{};
   lp.jobs = reinterpret_cast<const JobDev *>(base + kOffJob);
   lp.job_begin = reinterpret_cast<const int64_t *>(base + kOffBegin);
   lp.njobs = 1;

@@ -13,11 +13,10 @@
 
 namespace vmc {
 
-template <class R> __device__ __forceinline__ void start_rng(R &rng, const JobDev &J, int64_t q);
-template <> __device__ __forceinline__ void start_rng<PhiloxRng>(PhiloxRng &rng, const JobDev &J, int64_t q) {
+template <bool K> __device__ __forceinline__ void start_rng(PhiloxT<K> &rng, const JobDev &J, int64_t q) {
   rng.start(J.seed, J.stream, (uint64_t)(q + J.poffset));
 }
-template <> __device__ __forceinline__ void start_rng<TapeRng>(TapeRng &rng, const JobDev &J, int64_t q) {
+__device__ __forceinline__ void start_rng(TapeRng &rng, const JobDev &J, int64_t q) {
   rng.start_tape(J.tape + J.tape_off[q], J.tape + J.tape_off[q + 1]);
 }
 
@@ -31,12 +30,16 @@ __device__ __forceinline__ int find_job(const LaunchParams &lp, int64_t p) {
   return lo;
 }
 
+// R::kOneJob: a launch of one job, whose descriptor (lp.job0) and Philox round keys are read
+// from the kernel parameters (constant bank) rather than from global memory and registers.
 template <class W, class R>
-__global__ void __launch_bounds__(256, W::kMinBlocks) pool_kernel(const LaunchParams lp) {
+__global__ void __launch_bounds__(256, W::kMinBlocks) pool_kernel(const __grid_constant__ LaunchParams lp) {
   extern __shared__ __align__(16) unsigned char vmc_smem[];
+  constexpr bool kOne = R::kOneJob;
   W s;
   R rng;
-  const JobDev *J = lp.jobs;
+  if constexpr (kOne) rng.rk = lp.rk;
+  const JobDev *J = kOne ? &lp.job0 : lp.jobs;
   Stage stg{nullptr, nullptr, 0u};
   if constexpr (W::kStaged) {
     if (lp.stage_slots > 0) {
@@ -78,9 +81,9 @@ __global__ void __launch_bounds__(256, W::kMinBlocks) pool_kernel(const LaunchPa
       const int rank = __popc(need & lt_mask);
       if (((need >> lane) & 1u) && rank < avail) {
         const long long p = chunk_next + rank;
-        J = lp.jobs + (lp.njobs > 1 ? find_job(lp, p) : 0);
+        if constexpr (!kOne) J = lp.jobs + (lp.njobs > 1 ? find_job(lp, p) : 0);
         const long long q = p - J->pbegin;
-        start_rng<R>(rng, *J, q);
+        start_rng(rng, *J, q);
         s.launch(*J, rng, q);
         alive = true;
       }

@@ -20,10 +20,16 @@ __device__ __forceinline__ uint4 *philox_slot() {
   return slots + threadIdx.x;
 }
 
-struct PhiloxRng {
+// kLaunchKey: every photon of the launch has the same key (a launch of one job), and the
+// ten round keys are kernel parameters (rk, set by the kernel): the rounds read them from
+// the constant bank instead of running the key schedule per lane.  The stream is the same.
+template <bool kLaunchKey>
+struct PhiloxT {
+  static constexpr bool kOneJob = kLaunchKey;
   uint32_t c0, c2;  // photon index low word, block counter
   uint4 buf;
   int32_t n;
+  const uint32_t *rk;  // kLaunchKey: round keys k_r = key + r (W0, W1), r = 0..9
 
   __device__ __forceinline__ void start(uint64_t seed, uint32_t stream, uint64_t photon) {
     *philox_slot() = make_uint4((uint32_t)seed, (uint32_t)(seed >> 32), (uint32_t)(photon >> 32), stream);
@@ -35,7 +41,11 @@ struct PhiloxRng {
     uint32_t x0 = c0, x1 = k.z, x2 = c2, x3 = k.w, a = k.x, b = k.y;
 #pragma unroll
     for (int r = 0; r < 10; r++) {
-      if (r) { a += 0x9E3779B9u; b += 0xBB67AE85u; }
+      if constexpr (kLaunchKey) {
+        a = rk[2 * r]; b = rk[2 * r + 1];
+      } else if (r) {
+        a += 0x9E3779B9u; b += 0xBB67AE85u;
+      }
       uint32_t hi0 = __umulhi(0xD2511F53u, x0), lo0 = 0xD2511F53u * x0;
       uint32_t hi1 = __umulhi(0xCD9E8D57u, x2), lo1 = 0xCD9E8D57u * x2;
       uint32_t y0 = hi1 ^ x1 ^ a, y2 = hi0 ^ x3 ^ b;
@@ -59,8 +69,11 @@ struct PhiloxRng {
   // the previous block are dropped.
   __device__ __forceinline__ void align() { n = 0; }
 };
+using PhiloxRng = PhiloxT<false>;  // per-photon key (batched launches)
+using PhiloxOne = PhiloxT<true>;   // launch-wide key (one job)
 
 struct TapeRng {
+  static constexpr bool kOneJob = false;
   const uint32_t *p, *end;
   bool out;
   __device__ __forceinline__ void start_tape(const uint32_t *b, const uint32_t *e) { p = b; end = e; out = false; }

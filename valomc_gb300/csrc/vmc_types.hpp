@@ -141,6 +141,10 @@ struct LaunchParams {
   Ctl *ctl;
   int32_t stage_slots;        // > 0: per-CTA shared-memory staging of ER deposits (power of 2)
   int32_t pad;
+  // launches of one job (the kernels whose RNG has kOneJob): the job's descriptor and the
+  // ten Philox round keys of its seed, (lo, hi) per round
+  JobDev job0;
+  uint32_t rk[20];
 };
 
 // Shared-memory staging of element deposits: a direct-mapped table of stage_slots entries

@@ -347,8 +347,8 @@ struct Walk3D64 {
 // =====================================================================================
 template <bool FD, class R>
 struct Walk3D32 {
-  // 4 CTAs of 256 per SM (64 registers): the walk is latency bound and more resident
-  // warps beat the few spills (measured +7% over 3 CTAs on the 648k-tet phantom)
+  // 4 CTAs of 256 per SM (64 registers): the walk is latency bound and 32 resident warps
+  // per SM beat 24 (+7% on the 648k-tet phantom); 5 CTAs (48 registers) spill and lose
   static constexpr int kMinBlocks = 4;
   static constexpr bool kStaged = !FD;
   using Tr = typename TraceFor<R>::type;

@@ -154,8 +154,15 @@ __device__ __forceinline__ void create_photon_2d(const JobDev &J, R &rng, double
   }
 }
 
+// A reduction into a global FP64 accumulator.  The accumulators are plain device buffers,
+// so the address is converted to the global window once and the add is issued as a
+// fire-and-forget global reduction (no generic-address resolution, no returned value).
+__device__ __forceinline__ void red_global(double *p, double v) {
+  asm volatile("red.global.add.f64 [%0], %1;" :: "l"(__cvta_generic_to_global(p)), "d"(v));
+}
+
 __device__ __forceinline__ void add_d(double *p, double v) {
-  if (v != 0.0) atomicAdd(p, v);
+  if (v != 0.0) red_global(p, v);
 }
 
 // float -> double by bit manipulation on the integer pipe (exact for normal floats; zero
@@ -171,7 +178,7 @@ __device__ __forceinline__ double f2d_int(float x) {
 }
 
 __device__ __forceinline__ void add_f(double *p, float v) {
-  if (v != 0.0f) atomicAdd(p, f2d_int(v));
+  if (v != 0.0f) red_global(p, f2d_int(v));
 }
 
 // element deposit through the CTA's shared-memory stage when it holds (or can claim) the
@@ -188,7 +195,7 @@ __device__ __forceinline__ void add_staged(const Stage &S, double *ER, int el, f
       return;
     }
   }
-  atomicAdd(ER + el, d);
+  red_global(ER + el, d);
 }
 
 // ---- FP32 launch for the tracking form: same draws and sampling laws as CreatePhoton,
