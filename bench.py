@@ -427,8 +427,7 @@ def bench_batch(args):
     tets = sum(p.Ne for p in probs)
     photons = sum(p.Nphoton for p in probs)
     t0 = time.time()
-    small = [p.copy(Nphoton=max(1, p.Nphoton // 50)) for p in probs]
-    tuned = V.autotune(meshes, small, budget_s=6.0)
+    tuned = V.autotune(meshes, probs, budget_s=6.0)
     t_tune = time.time() - t0
     res = {}
     for graph in (False, True):

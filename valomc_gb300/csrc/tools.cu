@@ -129,7 +129,11 @@ int vmc_bench_fp64(int32_t device, double seconds, double *tflops_out) {
 }
 
 // Times each launch shape on a bounded share of the jobs' photons (all jobs scaled by the
-// same factor so the mix is kept) and keeps the fastest in photons per second.
+// same factor so the mix is kept) and keeps the fastest in photons per second.  A trial
+// must keep every lane of the pool busy for many photon lifetimes: on a short trial the
+// drain at the end of the launch (the longest walks) dominates the time and favours small
+// grids, which lose at full size.  The default shape (256 threads, chunk 32, full
+// occupancy) is kept unless another beats it by more than 2%.
 int vmc_autotune(vmc_mesh *const *meshes, const vmc_input *jobs, int32_t njobs, vmc_options *opt, double budget_s) {
   if (!meshes || !jobs || njobs <= 0 || !opt) return VMC_ERR_INVALID_ARGUMENT;
   const int prec = opt->precision;
@@ -184,13 +188,17 @@ int vmc_autotune(vmc_mesh *const *meshes, const vmc_input *jobs, int32_t njobs, 
     rate = (double)n / std::max(1e-9, lr.kernel_ms * 1e-3);
     return VMC_OK;
   };
+  int sms = 0;
+  s = select_device(opt->device, &sms);
+  if (s) return s;
+  const double min_photons = 16.0 * 2048.0 * (double)sms;  // 16 fills of a full SM's lanes
   double rate0 = 0;
-  double frac = std::min(1.0, 20000.0 / (double)total);
+  double frac = std::min(1.0, min_photons / (double)total);
   s = run(base, frac, rate0);
   if (s) return s;
   const double per_trial = std::max(0.02, budget_s / nshape);
-  frac = std::min(1.0, rate0 * per_trial / (double)total);
-  double best = -1;
+  frac = std::min(1.0, std::max(min_photons, rate0 * per_trial) / (double)total);
+  double best = -1, dflt = -1;
   LaunchSpec bsp = base;
   for (int b : blocks)
     for (int c : chunks)
@@ -207,8 +215,15 @@ int vmc_autotune(vmc_mesh *const *meshes, const vmc_input *jobs, int32_t njobs, 
         double rate = 0;
         s = run(sp, frac, rate);
         if (s) return s;
+        if (b == 256 && c == 32 && !half) dflt = rate;
         if (rate > best) { best = rate; bsp = sp; }
       }
+  if (dflt > 0 && best < 1.02 * dflt) {
+    bsp = base;
+    bsp.block = 256;
+    bsp.chunk = 32;
+    bsp.blocks_per_sm = 0;
+  }
   opt->block_size = bsp.block;
   opt->fetch_chunk = bsp.chunk;
   opt->blocks_per_sm = bsp.blocks_per_sm;
