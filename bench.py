@@ -485,10 +485,15 @@ def bench_serve(args):
     wall = time.time() - t0
     srv.close()
     offered = sum(n for _, n in sub) / args.serve_window
+    quarter = max(1, len(lat) // 4)
+    q_first, q_last = float(np.median(lat[:quarter])), float(np.median(lat[-quarter:]))
     out = {"metric": "serve p50/p99 latency and photons/s", "unit": "s", "rate_hz": args.serve_rate,
            "window_s": args.serve_window, "requests": len(sub), "submit_s": t_sub, "drain_s": wall - t_sub,
            "offered_photons_per_s": offered, "served_photons_per_s": ph / wall,
-           "stable": wall < 1.2 * args.serve_window + 2.0,
+           # stable: the device keeps up (served >= 95% of offered) and the latency does not
+           # grow over the window (median of the last quarter of requests vs the first)
+           "stable": bool(ph / wall >= 0.95 * offered and q_last <= 2.0 * q_first + 0.05),
+           "p50_first_quarter_s": q_first, "p50_last_quarter_s": q_last,
            "p50_s": float(np.percentile(lat, 50)), "p90_s": float(np.percentile(lat, 90)),
            "p99_s": float(np.percentile(lat, 99)), "value": float(np.percentile(lat, 99)),
            "config": {"workload": "8 cubes 50k-2M tets, cosinic disk / gaussian sources, photons logU[1e5,1e7]"}}

@@ -76,6 +76,30 @@ struct LaunchResult {
 int launch_jobs(int device, const LaunchSpec &spec, const std::vector<JobDev> &jobs, const vmc_options *opt,
                 cudaStream_t st, LaunchResult &res);
 
+// Device and pinned buffers of one launch at a time, reused across launches: the job
+// table, its photon prefix, the control block, the timing events and a graph.  Lets a
+// caller keep a launch in flight while it prepares the next on another arena and stream.
+struct LaunchArena {
+  JobDev *djobs = nullptr, *hjobs = nullptr;
+  int64_t *dbegin = nullptr, *hbegin = nullptr;
+  Ctl *dctl = nullptr, *hctl = nullptr;
+  size_t cap_jobs = 0;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaStream_t cap_stream = nullptr;  // graph capture
+  cudaGraphExec_t exec = nullptr;
+  int64_t total = 0;
+  bool pending = false;
+  LaunchArena() = default;
+  LaunchArena(const LaunchArena &) = delete;
+  LaunchArena &operator=(const LaunchArena &) = delete;
+  ~LaunchArena();
+};
+// Enqueues the pool kernel over jobs on `st` without waiting (no progress polling).
+int launch_start(int device, const LaunchSpec &spec, const std::vector<JobDev> &jobs, LaunchArena &a,
+                 cudaStream_t st, LaunchResult &res);
+// Waits for the arena's launch and reads its counters (no-op when nothing is in flight).
+int launch_finish(LaunchArena &a, cudaStream_t st, LaunchResult &res);
+
 // Copies a job's accumulators and counters back and fills out/stats.
 int collect_job(const HostJob &j, const DeviceMesh &m, const JobBuffers &b, int64_t nphoton, bool normalize,
                 vmc_output *out, vmc_stats *st, cudaStream_t stream);

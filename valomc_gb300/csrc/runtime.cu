@@ -308,37 +308,108 @@ GraphSlot &graph_slot(const void *fn, int grid, int block) {
 }
 }  // namespace
 
-int launch_jobs(int device, const LaunchSpec &spec, const std::vector<JobDev> &jobs_in, const vmc_options *opt,
-                cudaStream_t st, LaunchResult &res) {
+namespace {
+// What one launch needs before any buffer exists: the kernel, the grid, the job table with
+// its photon prefix.
+struct LaunchPlan {
+  const void *fn = nullptr;
+  bool one = false;
+  int grid = 0, block = 0, stage_slots = 0;
+  size_t smem = 0;
+  int64_t total = 0;
+  std::vector<JobDev> jobs;
+  std::vector<int64_t> begin;
+};
+
+int plan_launch(int device, const LaunchSpec &spec, const std::vector<JobDev> &jobs_in, LaunchPlan &p,
+                LaunchResult &res) {
   int sms = 0;
   VMC_TRY(select_device(device, &sms));
-  const bool one = jobs_in.size() == 1 && !spec.tape;
-  const void *fn = select_kernel(spec, one);
-  if (!fn) { set_error("no kernel for this configuration"); return VMC_ERR_INVALID_ARGUMENT; }
-  std::vector<JobDev> jobs = jobs_in;
-  std::vector<int64_t> begin(jobs.size() + 1, 0);
-  for (size_t i = 0; i < jobs.size(); i++) {
-    jobs[i].pbegin = begin[i];
-    begin[i + 1] = begin[i] + jobs[i].pcount;
+  p.one = jobs_in.size() == 1 && !spec.tape;
+  p.fn = select_kernel(spec, p.one);
+  if (!p.fn) { set_error("no kernel for this configuration"); return VMC_ERR_INVALID_ARGUMENT; }
+  p.jobs = jobs_in;
+  p.begin.assign(p.jobs.size() + 1, 0);
+  for (size_t i = 0; i < p.jobs.size(); i++) {
+    p.jobs[i].pbegin = p.begin[i];
+    p.begin[i + 1] = p.begin[i] + p.jobs[i].pcount;
   }
-  const int64_t total = begin.back();
+  p.total = p.begin.back();
   res = LaunchResult();
-  int block = spec.block > 0 ? spec.block : 256;
-  if (block % 32 || block > 256) { set_error("block size must be a multiple of 32, at most 256"); return VMC_ERR_INVALID_ARGUMENT; }
+  p.block = spec.block > 0 ? spec.block : 256;
+  if (p.block % 32 || p.block > 256) { set_error("block size must be a multiple of 32, at most 256"); return VMC_ERR_INVALID_ARGUMENT; }
   int per_sm = 0;
   // shared-memory staging of deposits: FP32 tetrahedral walk, continuous wave, one job
-  int stage_slots = 0;
-  if (spec.stage_slots > 0 && spec.dim == 3 && spec.precision == VMC_FP32 && !spec.fd && jobs.size() == 1) {
-    stage_slots = 1;
-    while (stage_slots < spec.stage_slots && stage_slots < 4096) stage_slots <<= 1;
+  p.stage_slots = 0;
+  if (spec.stage_slots > 0 && spec.dim == 3 && spec.precision == VMC_FP32 && !spec.fd && p.jobs.size() == 1) {
+    p.stage_slots = 1;
+    while (p.stage_slots < spec.stage_slots && p.stage_slots < 4096) p.stage_slots <<= 1;
   }
-  const size_t smem = (size_t)stage_slots * (sizeof(double) + sizeof(int32_t));
-  VMC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, smem));
+  p.smem = (size_t)p.stage_slots * (sizeof(double) + sizeof(int32_t));
+  VMC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, p.fn, p.block, p.smem));
   if (per_sm < 1) { set_error("kernel does not fit on an SM at this block size"); return VMC_ERR_INVALID_ARGUMENT; }
   if (spec.blocks_per_sm > 0) per_sm = std::min(per_sm, spec.blocks_per_sm);
-  const int grid = per_sm * sms;
-  res.grid = grid;
-  res.block = block;
+  p.grid = per_sm * sms;
+  res.grid = p.grid;
+  res.block = p.block;
+  return VMC_OK;
+}
+
+LaunchParams make_params(const LaunchSpec &spec, const LaunchPlan &p, const JobDev *djobs, const int64_t *dbegin,
+                         Ctl *dctl) {
+  LaunchParams lp{};
+  lp.jobs = djobs;
+  if (p.one) set_single_job(lp, p.jobs[0]);
+  lp.job_begin = dbegin;
+  lp.njobs = (int32_t)p.jobs.size();
+  lp.chunk = spec.chunk > 0 ? spec.chunk : 32;
+  lp.total = p.total;
+  lp.max_steps = spec.max_steps > 0 ? spec.max_steps : 10000000;
+  lp.ctl = dctl;
+  lp.stage_slots = p.stage_slots;
+  lp.pad = 0;
+  return lp;
+}
+
+// Records the control-block reset and the kernel as a graph on `cap` and updates `exec` in
+// place when it holds a graph of the same shape (else instantiates it anew).
+int capture_launch(cudaStream_t cap, const LaunchPlan &p, void **args, Ctl *dctl, cudaGraphExec_t &exec) {
+  VMC_CK(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+  cudaError_t ce = cudaMemsetAsync(dctl, 0, sizeof(Ctl), cap);
+  if (ce == cudaSuccess) ce = cudaLaunchKernel(p.fn, dim3(p.grid), dim3(p.block), args, p.smem, cap);
+  cudaGraph_t graph = nullptr;
+  cudaError_t ee = cudaStreamEndCapture(cap, &graph);
+  if (ce != cudaSuccess) { if (graph) cudaGraphDestroy(graph); return cuda_status(ce, "graph capture"); }
+  if (ee != cudaSuccess) return cuda_status(ee, "cudaStreamEndCapture");
+  bool updated = false;
+  if (exec) {
+    cudaGraphExecUpdateResultInfo info;
+    updated = cudaGraphExecUpdate(exec, graph, &info) == cudaSuccess;
+    if (!updated) {
+      cudaGetLastError();
+      cudaGraphExecDestroy(exec);
+      exec = nullptr;
+    }
+  }
+  if (!updated) {
+    cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+    if (ie != cudaSuccess) { cudaGraphDestroy(graph); exec = nullptr; return cuda_status(ie, "cudaGraphInstantiate"); }
+  }
+  cudaGraphDestroy(graph);
+  return VMC_OK;
+}
+}  // namespace
+
+int launch_jobs(int device, const LaunchSpec &spec, const std::vector<JobDev> &jobs_in, const vmc_options *opt,
+                cudaStream_t st, LaunchResult &res) {
+  LaunchPlan plan;
+  VMC_TRY(plan_launch(device, spec, jobs_in, plan, res));
+  const std::vector<JobDev> &jobs = plan.jobs;
+  const std::vector<int64_t> &begin = plan.begin;
+  const int64_t total = plan.total;
+  const void *fn = plan.fn;
+  const int grid = plan.grid, block = plan.block;
+  const size_t smem = plan.smem;
   if (total == 0) return VMC_OK;
 
   DevGuard<JobDev> djobs;
@@ -351,17 +422,7 @@ int launch_jobs(int device, const LaunchSpec &spec, const std::vector<JobDev> &j
   VMC_TRY(h2d(djobs.p, jobs.data(), jobs.size(), st));
   VMC_TRY(h2d(dbegin.p, begin.data(), begin.size(), st));
   VMC_CK(cudaMemsetAsync(dctl.p, 0, sizeof(Ctl), st));
-  LaunchParams lp{};
-  lp.jobs = djobs.p;
-  if (one) set_single_job(lp, jobs[0]);
-  lp.job_begin = dbegin.p;
-  lp.njobs = (int32_t)jobs.size();
-  lp.chunk = spec.chunk > 0 ? spec.chunk : 32;
-  lp.total = total;
-  lp.max_steps = spec.max_steps > 0 ? spec.max_steps : 10000000;
-  lp.ctl = dctl.p;
-  lp.stage_slots = stage_slots;
-  lp.pad = 0;
+  LaunchParams lp = make_params(spec, plan, djobs.p, dbegin.p, dctl.p);
   EventGuard e0, e1;
   VMC_CK(cudaEventCreate(&e0.e));
   VMC_CK(cudaEventCreate(&e1.e));
@@ -378,29 +439,8 @@ int launch_jobs(int device, const LaunchSpec &spec, const std::vector<JobDev> &j
     VMC_CK(cudaStreamCreateWithFlags(&gstream.s, cudaStreamNonBlocking));
     VMC_CK(cudaEventRecord(e0.e, st));
     VMC_CK(cudaStreamWaitEvent(gstream.s, e0.e, 0));
-    VMC_CK(cudaStreamBeginCapture(gstream.s, cudaStreamCaptureModeThreadLocal));
-    cudaError_t ce = cudaMemsetAsync(dctl.p, 0, sizeof(Ctl), gstream.s);
-    if (ce == cudaSuccess) ce = cudaLaunchKernel(fn, dim3(grid), dim3(block), args, smem, gstream.s);
-    cudaGraph_t graph = nullptr;
-    cudaError_t ee = cudaStreamEndCapture(gstream.s, &graph);
-    if (ce != cudaSuccess) { if (graph) cudaGraphDestroy(graph); return cuda_status(ce, "graph capture"); }
-    if (ee != cudaSuccess) return cuda_status(ee, "cudaStreamEndCapture");
     GraphSlot &slot = graph_slot(fn, grid, block);
-    bool updated = false;
-    if (slot.exec) {
-      cudaGraphExecUpdateResultInfo info;
-      updated = cudaGraphExecUpdate(slot.exec, graph, &info) == cudaSuccess;
-      if (!updated) {
-        cudaGetLastError();
-        cudaGraphExecDestroy(slot.exec);
-        slot.exec = nullptr;
-      }
-    }
-    if (!updated) {
-      cudaError_t ie = cudaGraphInstantiate(&slot.exec, graph, 0);
-      if (ie != cudaSuccess) { cudaGraphDestroy(graph); slot.exec = nullptr; return cuda_status(ie, "cudaGraphInstantiate"); }
-    }
-    cudaGraphDestroy(graph);
+    VMC_TRY(capture_launch(gstream.s, plan, args, dctl.p, slot.exec));
     VMC_CK(cudaEventRecord(e0.e, gstream.s));
     VMC_CK(cudaGraphLaunch(slot.exec, gstream.s));
     VMC_CK(cudaEventRecord(e1.e, gstream.s));
@@ -460,6 +500,91 @@ int launch_jobs(int device, const LaunchSpec &spec, const std::vector<JobDev> &j
   res.kernel_ms = ms;
   if (opt && opt->progress && status == VMC_OK) opt->progress(100.0, opt->progress_user);
   return status;
+}
+
+LaunchArena::~LaunchArena() {
+  if (djobs) cudaFree(djobs);
+  if (dbegin) cudaFree(dbegin);
+  if (dctl) cudaFree(dctl);
+  if (hjobs) cudaFreeHost(hjobs);
+  if (hbegin) cudaFreeHost(hbegin);
+  if (hctl) cudaFreeHost(hctl);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (exec) cudaGraphExecDestroy(exec);
+  if (cap_stream) cudaStreamDestroy(cap_stream);
+}
+
+int launch_start(int device, const LaunchSpec &spec, const std::vector<JobDev> &jobs_in, LaunchArena &a,
+                 cudaStream_t st, LaunchResult &res) {
+  if (a.pending) { set_error("arena has a launch in flight"); return VMC_ERR_INVALID_ARGUMENT; }
+  LaunchPlan plan;
+  VMC_TRY(plan_launch(device, spec, jobs_in, plan, res));
+  a.total = plan.total;
+  if (plan.total == 0) return VMC_OK;
+  const size_t nj = plan.jobs.size();
+  if (nj > a.cap_jobs) {
+    // grow the job table (device and pinned staging) to the next power of two
+    size_t cap = 16;
+    while (cap < nj) cap <<= 1;
+    if (a.djobs) { cudaFree(a.djobs); a.djobs = nullptr; }
+    if (a.dbegin) { cudaFree(a.dbegin); a.dbegin = nullptr; }
+    if (a.hjobs) { cudaFreeHost(a.hjobs); a.hjobs = nullptr; }
+    if (a.hbegin) { cudaFreeHost(a.hbegin); a.hbegin = nullptr; }
+    a.cap_jobs = 0;
+    int64_t bytes = 0;
+    VMC_TRY(dalloc(&a.djobs, cap, bytes));
+    VMC_TRY(dalloc(&a.dbegin, cap + 1, bytes));
+    VMC_CK(cudaMallocHost(reinterpret_cast<void **>(&a.hjobs), cap * sizeof(JobDev)));
+    VMC_CK(cudaMallocHost(reinterpret_cast<void **>(&a.hbegin), (cap + 1) * sizeof(int64_t)));
+    a.cap_jobs = cap;
+  }
+  if (!a.dctl) {
+    int64_t bytes = 0;
+    VMC_TRY(dalloc(&a.dctl, 1, bytes));
+    VMC_CK(cudaMallocHost(reinterpret_cast<void **>(&a.hctl), sizeof(Ctl)));
+    VMC_CK(cudaEventCreate(&a.e0));
+    VMC_CK(cudaEventCreate(&a.e1));
+  }
+  // the pinned staging is free: the previous launch of this arena has finished
+  memcpy(a.hjobs, plan.jobs.data(), nj * sizeof(JobDev));
+  memcpy(a.hbegin, plan.begin.data(), (nj + 1) * sizeof(int64_t));
+  VMC_TRY(h2d(a.djobs, a.hjobs, nj, st));
+  VMC_TRY(h2d(a.dbegin, a.hbegin, nj + 1, st));
+  LaunchParams lp = make_params(spec, plan, a.djobs, a.dbegin, a.dctl);
+  void *args[] = {&lp};
+  if (!spec.graph) {
+    VMC_CK(cudaMemsetAsync(a.dctl, 0, sizeof(Ctl), st));
+    VMC_CK(cudaEventRecord(a.e0, st));
+    VMC_CK(cudaLaunchKernel(plan.fn, dim3(plan.grid), dim3(plan.block), args, plan.smem, st));
+    VMC_CK(cudaEventRecord(a.e1, st));
+  } else {
+    // the arena's own graph: it is never updated while one of its launches is in flight
+    if (!a.cap_stream) VMC_CK(cudaStreamCreateWithFlags(&a.cap_stream, cudaStreamNonBlocking));
+    VMC_TRY(capture_launch(a.cap_stream, plan, args, a.dctl, a.exec));
+    VMC_CK(cudaEventRecord(a.e0, st));
+    VMC_CK(cudaGraphLaunch(a.exec, st));
+    VMC_CK(cudaEventRecord(a.e1, st));
+  }
+  a.pending = true;
+  return VMC_OK;
+}
+
+int launch_finish(LaunchArena &a, cudaStream_t st, LaunchResult &res) {
+  if (!a.pending) return VMC_OK;
+  a.pending = false;
+  VMC_CK(cudaEventSynchronize(a.e1));
+  VMC_CK(cudaGetLastError());
+  float ms = 0;
+  VMC_CK(cudaEventElapsedTime(&ms, a.e0, a.e1));
+  VMC_CK(cudaMemcpyAsync(a.hctl, a.dctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+  VMC_CK(cudaStreamSynchronize(st));
+  g_d2h_bytes += (int64_t)sizeof(Ctl);
+  res.steps = a.hctl->steps;
+  res.scatters = a.hctl->scatters;
+  res.done = a.hctl->done_photons;
+  res.kernel_ms = ms;
+  return VMC_OK;
 }
 
 int collect_job(const HostJob &j, const DeviceMesh &m, const JobBuffers &b, int64_t nphoton, bool normalize,

@@ -2,6 +2,9 @@
 // device-memory footprint, continuous batching of all admitted requests into short
 // persistent launches ("epochs").
 //
+// Epochs alternate between two streams ("lanes"): the next epoch is queued while the
+// current one runs, so it takes the SMs as the running launch drains.
+//
 // A request's photons are issued in slices across epochs; slice k of a request simulates
 // photon indices [issued, issued + quota) of the request's own Philox stream (key = the
 // request seed, counter = photon index), so the photons and their draws do not depend on
@@ -45,6 +48,8 @@ struct Request {
   std::unique_ptr<JobBuffers> buf;
   int state = kQueued;
   int status = VMC_OK;
+  int inflight = 0;  // launches holding a slice of this request
+  bool retiring = false;
   Clock::time_point t_submit, t_admit, t_finish;
   double kernel_s = 0;
   std::vector<double> ER, EI, EBR, EBI, DEBR, DEBI;
@@ -66,19 +71,55 @@ struct vmc_server {
   double rate = 0;  // photons per second seen in recent epochs
   bool stop = false;
   std::thread worker;
+  // Finished requests wait here for their results to be copied back and normalised by the
+  // collector thread, so that the launch loop never stops for a read-back.
+  std::deque<Request *> to_collect;
+  std::condition_variable cv_collect;
+  bool collector_stop = false;
+  std::thread collector;
   void loop();
+  void collect_loop();
+  void finalize(Request *r);
 };
+
+namespace {
+// One of the two launch pipelines of the serving loop: a stream, an arena per launch class
+// (dimension x CW/FD) and the requests whose slices ride in its current epoch.
+struct Lane {
+  cudaStream_t st = nullptr;
+  std::vector<std::unique_ptr<LaunchArena>> arenas;
+  std::vector<std::vector<Request *>> members;  // per arena: the requests of its launch
+  std::vector<std::vector<int64_t>> quotas;
+  bool pending = false;
+  double photons = 0;
+};
+}  // namespace
 
 void vmc_server::loop() {
   cudaSetDevice(cfg.device);
-  cudaStream_t st = 0;
+  // Two lanes: while an epoch runs on one, the next is prepared and queued on the other,
+  // so its CTAs take the SMs as the running launch drains (no idle tail between epochs).
+  Lane lanes[2];
+  for (auto &l : lanes) cudaStreamCreateWithFlags(&l.st, cudaStreamNonBlocking);
+  Clock::time_point last_finish = Clock::now();
+  int cur = 0;
   for (;;) {
     std::vector<Request *> admitted;
     std::vector<Request *> batch;
     {
       std::unique_lock<std::mutex> lk(mu);
-      cv_work.wait(lk, [&] { return stop || !queue.empty() || !active.empty(); });
-      if (stop) return;
+      auto has_work = [&] {
+        // a queued request that can be admitted now (or refused: larger than the budget)
+        if (!queue.empty() && (int)active.size() < cfg.max_slots &&
+            (queue.front()->footprint > cfg.memory_budget ||
+             mem_in_use + queue.front()->footprint <= cfg.memory_budget))
+          return true;
+        for (Request *r : active)
+          if (r->status == VMC_OK && r->issued < r->nphoton) return true;
+        return false;
+      };
+      if (!lanes[0].pending && !lanes[1].pending) cv_work.wait(lk, [&] { return stop || has_work(); });
+      if (stop) break;
       // admission: FIFO while a slot is free and the footprint fits the budget
       while (!queue.empty() && (int)active.size() < cfg.max_slots) {
         Request *r = queue.front();
@@ -100,19 +141,26 @@ void vmc_server::loop() {
       }
       batch = active;
     }
+    Lane &L = lanes[cur];
+    // L's previous epoch has finished (it was the other lane one iteration ago), so its
+    // stream is idle: upload the new requests there and wait for the copies, which orders
+    // them before any launch on either lane.
     for (Request *r : admitted) {
       r->buf.reset(new JobBuffers);
       DeviceMesh *m = mesh_impl(meshes[(size_t)r->mesh_id]);
-      r->status = upload_job(r->job, *m, cfg.precision, *r->buf, st);
+      r->status = upload_job(r->job, *m, cfg.precision, *r->buf, L.st);
     }
-    // epoch: a slice of every active request, in as many launches as there are classes
+    if (!admitted.empty()) cudaStreamSynchronize(L.st);
+    // epoch: a slice of every active request with photons left, one launch per class
     int64_t epoch = cfg.epoch_photons > 0 ? cfg.epoch_photons
                                           : std::max<int64_t>(200000, (int64_t)(rate * 0.05));
-    const int64_t share = std::max<int64_t>(1, epoch / (int64_t)std::max<size_t>(1, batch.size()));
+    std::vector<Request *> open;
+    for (Request *r : batch)
+      if (r->status == VMC_OK && r->issued < r->nphoton) open.push_back(r);
+    const int64_t share = std::max<int64_t>(1, epoch / (int64_t)std::max<size_t>(1, open.size()));
     struct Cls { int dim; bool fd; std::vector<Request *> rs; };
     std::vector<Cls> classes;
-    for (Request *r : batch) {
-      if (r->status != VMC_OK) continue;
+    for (Request *r : open) {
       DeviceMesh *m = mesh_impl(meshes[(size_t)r->mesh_id]);
       bool fd = r->job.omega > 0;
       Cls *c = nullptr;
@@ -121,8 +169,12 @@ void vmc_server::loop() {
       if (!c) { classes.push_back(Cls{m->host.dim, fd, {}}); c = &classes.back(); }
       c->rs.push_back(r);
     }
-    double epoch_ph = 0, epoch_s = 0;
-    for (auto &c : classes) {
+    L.members.assign(classes.size(), {});
+    L.quotas.assign(classes.size(), {});
+    while (L.arenas.size() < classes.size()) L.arenas.emplace_back(new LaunchArena);
+    L.photons = 0;
+    for (size_t k = 0; k < classes.size(); k++) {
+      Cls &c = classes[k];
       std::vector<JobDev> descs;
       std::vector<int64_t> quota;
       for (Request *r : c.rs) {
@@ -142,50 +194,115 @@ void vmc_server::loop() {
       sp.blocks_per_sm = cfg.blocks_per_sm;
       sp.graph = cfg.use_graph != 0;
       LaunchResult lr;
-      int s = launch_jobs(cfg.device, sp, descs, nullptr, st, lr);
+      int st = launch_start(cfg.device, sp, descs, *L.arenas[k], L.st, lr);
       for (size_t i = 0; i < c.rs.size(); i++) {
         Request *r = c.rs[i];
-        if (s != VMC_OK) { r->status = s; continue; }
+        if (st != VMC_OK) { r->status = st; continue; }
         r->issued += quota[i];
-        r->kernel_s += lr.kernel_ms * 1e-3;
+        r->inflight++;
+        L.photons += (double)quota[i];
       }
-      if (s == VMC_OK) {
-        for (int64_t q : quota) epoch_ph += (double)q;
-        epoch_s += lr.kernel_ms * 1e-3;
+      if (st == VMC_OK) {
+        L.members[k] = c.rs;
+        L.quotas[k] = quota;
+        L.pending = true;
       }
     }
-    if (epoch_s > 0) rate = epoch_ph / epoch_s;
-    // retire finished (or failed) requests
+    // finish the other lane's epoch (queued ahead of this one) and retire what it completed
+    Lane &O = lanes[cur ^ 1];
+    if (O.pending) {
+      O.pending = false;
+      std::vector<int> ok(O.members.size(), VMC_OK);
+      for (size_t k = 0; k < O.members.size(); k++) {
+        if (O.members[k].empty()) continue;
+        LaunchResult lr;
+        ok[k] = launch_finish(*O.arenas[k], O.st, lr);
+      }
+      auto now = Clock::now();
+      // Epochs overlap, so a request's device time is counted as the disjoint intervals
+      // between successive epoch ends, from its submission on.
+      for (size_t k = 0; k < O.members.size(); k++)
+        for (Request *r : O.members[k]) {
+          r->inflight--;
+          if (ok[k] != VMC_OK) r->status = ok[k];
+          r->kernel_s += std::chrono::duration<double>(now - std::max(last_finish, r->t_submit)).count();
+        }
+      const double dt = std::chrono::duration<double>(now - last_finish).count();
+      if (dt > 0 && O.photons > 0) rate = O.photons / dt;
+      last_finish = now;
+      O.members.clear();
+    } else {
+      last_finish = Clock::now();  // the device was idle: the rate clock starts now
+    }
+    // retire finished (or failed) requests that have no slice in flight: the results of
+    // finished ones go to the collector thread
     std::vector<Request *> fin;
     for (Request *r : batch)
-      if (r->status != VMC_OK || r->issued >= r->nphoton) fin.push_back(r);
+      if (r->inflight == 0 && !r->retiring && (r->status != VMC_OK || r->issued >= r->nphoton)) fin.push_back(r);
     for (Request *r : fin) {
+      r->retiring = true;
       if (r->status == VMC_OK) {
-        DeviceMesh *m = mesh_impl(meshes[(size_t)r->mesh_id]);
-        const int64_t Ne = m->host.Ne, Nb = m->host.Nb;
-        r->ER.resize((size_t)Ne); r->EI.resize((size_t)Ne);
-        r->EBR.resize((size_t)Nb); r->EBI.resize((size_t)Nb); r->DEBR.resize((size_t)Nb); r->DEBI.resize((size_t)Nb);
-        vmc_output o;
-        memset(&o, 0, sizeof(o));
-        o.ER = r->ER.data(); o.EI = r->EI.data(); o.EBR = r->EBR.data(); o.EBI = r->EBI.data();
-        o.DEBR = r->DEBR.data(); o.DEBI = r->DEBI.data();
-        r->stats.photons_requested = r->nphoton;
-        r->stats.photons_done = r->issued;
-        r->stats.seed_used = r->job.seed;
-        r->status = collect_job(r->job, *m, *r->buf, r->nphoton, true, &o, &r->stats, st);
+        std::lock_guard<std::mutex> lk(mu);
+        to_collect.push_back(r);
+        cv_collect.notify_one();
+      } else {
+        finalize(r);
       }
-      r->buf.reset();
-      std::lock_guard<std::mutex> lk(mu);
-      mem_in_use -= r->footprint;
-      r->t_finish = Clock::now();
-      r->state = r->status == VMC_OK ? kFinished : kFailed;
-      r->stats.seconds_kernel = r->kernel_s;
-      r->stats.seconds_setup = std::chrono::duration<double>(r->t_admit - r->t_submit).count();
-      r->stats.seconds_total = std::chrono::duration<double>(r->t_finish - r->t_submit).count();
-      active.erase(std::find(active.begin(), active.end(), r));
     }
-    if (!fin.empty()) cv_done.notify_all();
+    cur ^= 1;
   }
+  // stopping: let launches in flight end before their buffers go
+  for (auto &l : lanes) {
+    if (l.st) cudaStreamSynchronize(l.st);
+    l.arenas.clear();
+    if (l.st) cudaStreamDestroy(l.st);
+  }
+}
+
+void vmc_server::finalize(Request *r) {
+  r->buf.reset();
+  std::lock_guard<std::mutex> lk(mu);
+  mem_in_use -= r->footprint;
+  r->t_finish = Clock::now();
+  r->state = r->status == VMC_OK ? kFinished : kFailed;
+  r->stats.seconds_kernel = r->kernel_s;
+  r->stats.seconds_setup = std::chrono::duration<double>(r->t_admit - r->t_submit).count();
+  r->stats.seconds_total = std::chrono::duration<double>(r->t_finish - r->t_submit).count();
+  active.erase(std::find(active.begin(), active.end(), r));
+  cv_done.notify_all();
+  cv_work.notify_all();  // memory and a slot were freed
+}
+
+void vmc_server::collect_loop() {
+  cudaSetDevice(cfg.device);
+  cudaStream_t st = nullptr;
+  cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+  for (;;) {
+    Request *r = nullptr;
+    {
+      std::unique_lock<std::mutex> lk(mu);
+      cv_collect.wait(lk, [&] { return collector_stop || !to_collect.empty(); });
+      if (to_collect.empty()) break;  // stopping and nothing left
+      r = to_collect.front();
+      to_collect.pop_front();
+    }
+    // the request's last launch has completed (the loop saw its event), so its
+    // accumulators are final
+    DeviceMesh *m = mesh_impl(meshes[(size_t)r->mesh_id]);
+    const int64_t Ne = m->host.Ne, Nb = m->host.Nb;
+    r->ER.resize((size_t)Ne); r->EI.resize((size_t)Ne);
+    r->EBR.resize((size_t)Nb); r->EBI.resize((size_t)Nb); r->DEBR.resize((size_t)Nb); r->DEBI.resize((size_t)Nb);
+    vmc_output o;
+    memset(&o, 0, sizeof(o));
+    o.ER = r->ER.data(); o.EI = r->EI.data(); o.EBR = r->EBR.data(); o.EBI = r->EBI.data();
+    o.DEBR = r->DEBR.data(); o.DEBI = r->DEBI.data();
+    r->stats.photons_requested = r->nphoton;
+    r->stats.photons_done = r->issued;
+    r->stats.seed_used = r->job.seed;
+    r->status = collect_job(r->job, *m, *r->buf, r->nphoton, true, &o, &r->stats, st);
+    finalize(r);
+  }
+  cudaStreamDestroy(st);
 }
 
 extern "C" {
@@ -198,6 +315,7 @@ int vmc_server_create(const vmc_server_config *cfg, vmc_server **out) {
   vmc_server *sv = new vmc_server;
   sv->cfg = *cfg;
   sv->worker = std::thread([sv] { sv->loop(); });
+  sv->collector = std::thread([sv] { sv->collect_loop(); });
   *out = sv;
   return VMC_OK;
 }
@@ -291,6 +409,12 @@ int vmc_server_destroy(vmc_server *s) {
     s->cv_work.notify_all();
   }
   if (s->worker.joinable()) s->worker.join();
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->collector_stop = true;
+    s->cv_collect.notify_all();
+  }
+  if (s->collector.joinable()) s->collector.join();
   for (auto &kv : s->all) kv.second->buf.reset();
   delete s;
   return VMC_OK;
