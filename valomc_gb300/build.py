@@ -22,7 +22,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_UNITS = ["kern3d32.cu", "kern3d64.cu", "kern2d32.cu", "kern2d64.cu", "runtime.cu", "tools.cu", "server.cu",
             "noalloc.cu"]
 CPP_UNITS = ["host_setup.cpp"]
-APPS = {"MC3D": "app/mc3d_main.cpp", "MC2D": "app/mc2d_main.cpp"}
+APPS = {"MC3D": "app/mc3d_main.cpp", "MC2D": "app/mc2d_main.cpp", "vmc_textdump": "app/textdump.cpp"}
 
 
 def nvcc():
@@ -78,7 +78,7 @@ def build(force=False, verbose=False, jobs=None):
     for app, src in APPS.items():
         path = os.path.join(CSRC, src)
         if os.path.exists(path):
-            _run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I" + INCLUDE, path, "-o", os.path.join(BUILD, app),
+            _run(["g++", "-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-I" + INCLUDE, path, "-o", os.path.join(BUILD, app),
                   "-L" + BUILD, "-lvalomc_gb300", "-Wl,-rpath,$ORIGIN"])
     return LIB
 
