@@ -88,6 +88,16 @@ def build(quiet=True):
     subprocess.run(cmd, check=True, capture_output=quiet)
 
 
+# the reference tree, where the checker's recipes read it (the Makefile's REF)
+REF_TREE = os.environ.get("REF", "/root/reference")
+
+
+def reference_file(rel):
+    """Path of a file of the reference tree, or None where the tree is absent."""
+    path = os.path.join(REF_TREE, rel)
+    return path if os.path.exists(path) else None
+
+
 def have_reference_binaries() -> bool:
     return all(os.path.exists(os.path.join(REF_DIR, b)) for b in ("ref3d_run", "ref2d_run", "ref3d_trace", "ref2d_trace"))
 

@@ -6,7 +6,7 @@ oracle/ref_harness.cpp).  This script needs that tree and those binaries; the fi
 writes are what the tests use everywhere else, so nothing at test time needs the
 reference.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]
 
 Fixtures (numpy .npz, float64 at full precision):
   run_<case>.npz    MonteCarlo() output of the reference with MT19937, given thread count
@@ -73,6 +73,9 @@ def cases():
         "mixed2d": (mixed_2d(), 2),
         "mixed2d_fd": (mixed_2d(f=1e8), 1),
         "pencil3d": (mg.pencil_box(8, 0.05, 12.0, 0.85, 1.4, (3.3, 4.45), 2000, seed=11), 1),
+        # uneven meshes: jittered nodes, random cell diagonals, boundaries from createBH
+        "circles2d": (mg.circles_2d(nphoton=20000, seed=321), 2),
+        "jitter3d": (mg.jittered_box_3d(nphoton=3000, seed=654), 2),
     }
 
 
@@ -82,21 +85,26 @@ def tape_for(case, nphot=24, words=6000, seed=424242):
     return tape, np.arange(nphot + 1, dtype=np.int64) * words
 
 
-TRACE_CASES = ["phantom3d", "mixed3d", "mixed3d_fd", "pencil3d", "square2d", "mixed2d", "mixed2d_fd"]
+TRACE_CASES = ["phantom3d", "mixed3d", "mixed3d_fd", "pencil3d", "square2d", "mixed2d", "mixed2d_fd", "circles2d",
+               "jitter3d"]
 
 
-def main():
+def main(only=None):
     import oracle
     oracle.build()
     if not oracle.have_reference_binaries():
         raise SystemExit("oracle/_ref/ binaries are missing: the reference tree is needed to make fixtures")
     for name, (p, nthr) in cases().items():
+        if only and name not in only:
+            continue
         out = oracle.ref_run(p, nthreads=nthr)
         assert out["status"] == 0, (name, out)
         np.savez_compressed(os.path.join(HERE, f"run_{name}.npz"), threads=nthr, loss=out["loss"],
                             **{k: out[k] for k in ("ER", "EI", "EBR", "EBI", "DEBR", "DEBI")})
         print(name, "threads", nthr, "loss", out["loss"])
     for name in TRACE_CASES:
+        if only and name not in only:
+            continue
         p = cases()[name][0]
         tape, off = tape_for(name)
         tr, used, acc = oracle.ref_trace(p, tape, off)
@@ -108,4 +116,5 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    # optional case names: regenerate only those fixtures
+    main(set(sys.argv[1:]) or None)

@@ -360,6 +360,76 @@ class ServingMix:
 # text format of the external executables
 # ---------------------------------------------------------------------------
 
+def uneven_mesh_2d(n=20, size=10.0, jitter=0.3, seed=6):
+    """An unstructured-looking triangle mesh of the square [-size/2, size/2]^2: an n x n grid
+    whose interior nodes are moved by up to jitter x h and whose cells are split along a
+    random diagonal, so element shapes, sizes and node valences (4-8) vary.  The boundary
+    is built by createBH (meshio.create_bh)."""
+    from .meshio import create_bh
+    rng = np.random.default_rng(seed)
+    h = size / n
+    g = np.linspace(-size / 2, size / 2, n + 1)
+    X, Y = np.meshgrid(g, g, indexing="ij")
+    r = np.stack([X.ravel(), Y.ravel()], axis=1)
+    inner = (np.abs(r[:, 0]) < size / 2 - 1e-9) & (np.abs(r[:, 1]) < size / 2 - 1e-9)
+    r[inner] += rng.uniform(-jitter * h, jitter * h, size=(int(inner.sum()), 2))
+    node = lambda i, j: i * (n + 1) + j
+    H = []
+    for i in range(n):
+        for j in range(n):
+            a, b, c, d = node(i, j), node(i + 1, j), node(i + 1, j + 1), node(i, j + 1)
+            if rng.random() < 0.5:
+                H += [[a, b, c], [a, c, d]]
+            else:
+                H += [[a, b, d], [b, c, d]]
+    H = np.asarray(H, np.int64)
+    return r, H, create_bh(H)
+
+
+def circles_2d(nphoton=20000, seed=12345):
+    """Two circular inclusions (n 1.5, mua 0.09, g 0.5) in a scattering square (n 1.3,
+    mua 0.01, mus 1.3, g 0.9) on an uneven mesh, air outside (Fresnel at the boundary), a
+    cosinic source on the left edge -- the optics of the reference's NetGen example
+    (examples/netgentest.m) on a mesh made here."""
+    r, H, BH = uneven_mesh_2d()
+    cen = r[H].mean(axis=1)
+    inc = (np.hypot(cen[:, 0] + 2.0, cen[:, 1] + 1.5) < 1.6) | (np.hypot(cen[:, 0] - 2.2, cen[:, 1] - 1.8) < 1.2)
+    ne, nb = len(H), len(BH)
+    mua = np.where(inc, 0.09, 0.01)
+    mus = np.full(ne, 1.3)
+    g = np.where(inc, 0.5, 0.9)
+    n = np.where(inc, 1.5, 1.3)
+    mid = r[BH].mean(axis=1)
+    types = np.full(nb, ord("a"), np.uint8)
+    types[mid[:, 0] < -5.0 + 1e-9] = ord("c")
+    return Problem(dim=2, H=H, BH=BH, r=r, mua=mua, mus=mus, g=g, n=n, BCType=types, BCn=np.ones(nb),
+                   Nphoton=nphoton, seed=seed)
+
+
+def jittered_box_3d(nphoton=3000, seed=12345, gen_seed=8):
+    """An 8 x 8 x 6 mm box of tets whose interior nodes are moved by up to 0.25 mm, with a
+    spherical inclusion (n 1.5) in n 1.37 tissue, air outside, a direct source on the
+    top-face triangles near the centre; boundary built by createBH3 (meshio.create_bh)."""
+    from .meshio import create_bh
+    r, H, _ = box_mesh_3d(8, 8, 6)
+    rng = np.random.default_rng(gen_seed)
+    lo, hi = r.min(axis=0), r.max(axis=0)
+    inner = np.all((r > lo + 1e-9) & (r < hi - 1e-9), axis=1)
+    r = r.copy()
+    r[inner] += rng.uniform(-0.25, 0.25, size=(int(inner.sum()), 3))
+    BH = create_bh(H)
+    cen = r[H].mean(axis=1)
+    inc = np.linalg.norm(cen - np.array([4.0, 4.0, 2.5]), axis=1) < 1.5
+    ne, nb = len(H), len(BH)
+    mid = r[BH].mean(axis=1)
+    types = np.full(nb, ord("a"), np.uint8)
+    top = (np.abs(mid[:, 2] - lo[2]) < 1e-9) & (np.hypot(mid[:, 0] - 4.0, mid[:, 1] - 4.0) < 1.5)
+    types[top] = ord("l")
+    return Problem(dim=3, H=H, BH=BH, r=r, mua=np.where(inc, 0.2, 0.02), mus=np.where(inc, 3.0, 6.0),
+                   g=np.where(inc, 0.6, 0.85), n=np.where(inc, 1.5, 1.37), BCType=types, BCn=np.ones(nb),
+                   Nphoton=nphoton, seed=seed)
+
+
 def write_input(path, p: Problem, nxyz=None, dirtype_tag=None):
     """The executables' input file (cpp/3d/MC3D.cpp:97-179, cpp/2d/MC2D.cpp:125-203,
     written like ValoMC.m:200-258,293-336)."""
