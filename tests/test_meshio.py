@@ -78,6 +78,21 @@ def test_vol_round_trip(maker):
     assert rowset(b.BH[b.boundaries[2]]) == rowset(p.BH[boundaries[2]])
 
 
+def test_grid_fluence_averages_each_pixel_and_voxel():
+    # a field constant per cell, given in MATLAB image order [y, x(, z)], comes back as is
+    r, H, _ = mg.rectangular_mesh(6, 4, 1.0)
+    c = r[H].mean(axis=1)
+    ix, iy = np.floor(c[:, 0] + 3).astype(int), np.floor(c[:, 1] + 2).astype(int)
+    f2 = np.random.default_rng(1).normal(size=(4, 6))
+    np.testing.assert_allclose(mg.grid_fluence(f2[iy, ix], 4, 6), f2)
+    r, H, _ = mg.box_mesh_3d(5, 4, 3)
+    v = np.floor(r[H].mean(axis=1)).astype(int)
+    f3 = np.random.default_rng(0).normal(size=(4, 5, 3))
+    np.testing.assert_allclose(mg.grid_fluence(f3[v[:, 1], v[:, 0], v[:, 2]], 4, 5, 3), f3)
+    with pytest.raises(ValueError):
+        mg.grid_fluence(np.zeros(10), 4, 5, 3)
+
+
 needs_vol = pytest.mark.skipif(REF_VOL is None, reason="reference example mesh not present")
 
 

@@ -195,6 +195,24 @@ def box_mesh_3d(nx, ny, nz, dh=1.0, origin=(0.0, 0.0, 0.0)):
     return grid_mesh_3d(xv, yv, zv)
 
 
+def grid_fluence(element_fluence, nx, ny, nz=None):
+    """ValoMC.m:266-271 / :340-351: the element fluence of a grid mesh (grid_mesh_2d: two
+    triangles per pixel; grid_mesh_3d: six tetrahedra per voxel) averaged per pixel / voxel.
+    nx, ny, nz are the sizes of the medium arrays' dimensions (createMedium.m:69-72, MATLAB
+    image order): for a mesh from grid_mesh_2d / grid_mesh_3d(xvec, yvec[, zvec]) they are
+    len(yvec), len(xvec)[, len(zvec)], and the result is indexed [y, x(, z)].  The mesh lists
+    its elements in blocks, one per sub-element of every cell, each block in column-major
+    cell order; each block is reshaped in that order and the blocks are averaged."""
+    x = np.asarray(element_fluence)
+    shape = (nx, ny) if nz is None else (nx, ny, nz)
+    ncell = int(np.prod(shape))
+    parts = 2 if nz is None else 6
+    if x.shape[0] != parts * ncell:
+        raise ValueError(f"{x.shape[0]} elements is not {parts} x {ncell} cells")
+    blocks = [x[k * ncell:(k + 1) * ncell].reshape(shape, order="F") for k in range(parts)]
+    return sum(blocks) / parts
+
+
 # ---------------------------------------------------------------------------
 # named workloads
 # ---------------------------------------------------------------------------
