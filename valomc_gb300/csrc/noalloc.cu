@@ -160,6 +160,7 @@ extern "C" int vmc_run_noalloc(vmc_mesh *mesh, const vmc_input *job, const vmc_o
   d.bnorm = m->d_bnorm;
   d.omega = hj.omega;
   d.k_scale = hj.k_scale;
+  d.k_scale_f = (float)hj.k_scale;
   d.phase0 = hj.phase0;
   d.seed = hj.seed;
   d.stream = o.stream_id;

@@ -218,6 +218,7 @@ JobDev describe_job(const HostJob &j, const DeviceMesh &m, int precision, const 
   d.bnorm = m.d_bnorm;
   d.omega = j.omega;
   d.k_scale = j.k_scale;
+  d.k_scale_f = (float)j.k_scale;
   d.phase0 = j.phase0;
   d.seed = j.seed;
   d.ER = b.d_acc;

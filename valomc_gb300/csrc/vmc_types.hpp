@@ -105,6 +105,8 @@ struct JobDev {
   const double *bnorm;         // [Nb x 4] Normal(ib) for MirrorPhoton (FP64 forms)
   double omega;                // 2 pi f
   double k_scale;              // omega / c0: k = k_scale * n  (cpp/3d/MC3D.hpp:662)
+  float k_scale_f;             // the same in FP32, for the tracking form
+  float pad_k;
   double phase0;
   uint64_t seed;
   uint32_t stream;

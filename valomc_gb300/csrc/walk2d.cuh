@@ -279,7 +279,7 @@ struct Walk2D32 {
       outward = ln.x * dx + ln.y * dy > 0.0f;
     }
     w = 1.0f;
-    phase = (float)J.phase0;
+    phase = fmodf((float)J.phase0, kTwoPiF);
     float4 o = optics(J, el);
     mua = o.x; mus = o.y; g = o.z; nidx = o.w;
     prop = free_path_f(unif_open_f(rng), mus);
@@ -400,17 +400,17 @@ struct Walk2D32 {
         acc += w * ds;
       }
     } else {
-      float th = (float)J.k_scale * nidx * ds;
-      float a = expf(-x);
-      float om = -expm1f(-x);
-      float sh = sinf(0.5f * th);
-      float c1 = om + 2.0f * a * sh * sh;
-      float s1 = a * sinf(th);
+      const float th = J.k_scale_f * nidx * ds;
+      const float om = one_minus_exp_neg(x);
+      const float a = 1.0f - om;
+      const float sh = sin_small(0.5f * th);
+      const float c1 = om + 2.0f * a * sh * sh;
+      const float s1 = a * sin_small(th);
       float sp, cp;
-      sincosf(phase, &sp, &cp);
+      __sincosf(phase, &sp, &cp);
       acc += w * (cp * c1 + sp * s1);
       accI += w * (cp * s1 - sp * c1);
-      phase += th;
+      phase = wrap_phase(phase + th);
       w *= a;
     }
     prop -= ds;
