@@ -477,11 +477,12 @@ def bench_serve(args):
             time.sleep(t - now)
         sub.append((srv.submit(ids[k], p), p.Nphoton))
     t_sub = time.time() - t0
-    lat, ph = [], 0
+    lat, ph, steps = [], 0, 0
     for rid, n in sub:
         r = srv.wait(rid)
         lat.append(r.stats["seconds_total"])
         ph += n
+        steps += r.stats["steps"]
     wall = time.time() - t0
     srv.close()
     offered = sum(n for _, n in sub) / args.serve_window
@@ -490,6 +491,7 @@ def bench_serve(args):
     out = {"metric": "serve p50/p99 latency and photons/s", "unit": "s", "rate_hz": args.serve_rate,
            "window_s": args.serve_window, "requests": len(sub), "submit_s": t_sub, "drain_s": wall - t_sub,
            "offered_photons_per_s": offered, "served_photons_per_s": ph / wall,
+           "served_steps_per_s": steps / wall, "steps_per_photon": steps / max(ph, 1),
            # stable: the device keeps up (served >= 95% of offered) and the latency does not
            # grow over the window (median of the last quarter of requests vs the first)
            "stable": bool(ph / wall >= 0.95 * offered and q_last <= 2.0 * q_first + 0.05),

@@ -36,6 +36,8 @@ def test_batch_equals_individual_runs(built, precision):
         one = V.run(p, precision=precision)
         np.testing.assert_allclose(r.ER, one.ER, rtol=RTOL, atol=1e-300)
         np.testing.assert_allclose(r.EBR, one.EBR, rtol=RTOL, atol=1e-300)
+        assert r.stats["steps"] == one.stats["steps"] > 0  # per-job step counts
+    assert sum(r.stats["steps"] for r in res) == tot["steps"]
 
 
 def test_batch_through_a_cuda_graph_equals_the_plain_launch(built):
@@ -89,6 +91,7 @@ def test_server_result_alone_equals_result_in_the_mix(built, precision):
         np.testing.assert_allclose(a.ER, one.ER, rtol=RTOL, atol=1e-300)
         np.testing.assert_allclose(m.EBR, one.EBR, rtol=RTOL, atol=1e-300)
         assert m.stats["photons_done"] == p.Nphoton
+        assert a.stats["steps"] == m.stats["steps"] == one.stats["steps"]
 
 
 def test_server_admission_by_memory_footprint(built):

@@ -99,6 +99,7 @@ __global__ void __launch_bounds__(256, W::kMinBlocks) pool_kernel(const __grid_c
         if (r == kDied) n_steps++;
         alive = false;
         n_done++;
+        job_count_add(*J, kJcSteps, (unsigned long long)s.nsteps);
       }
     }
   }

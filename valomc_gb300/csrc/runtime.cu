@@ -608,6 +608,7 @@ int collect_job(const HostJob &j, const DeviceMesh &m, const JobBuffers &b, int6
       for (int k = 0; k < kJcN; k++) c[k] += jc[(size_t)s * kJcN + k];
       for (int k = 0; k < kLgN; k++) L[k] += lg[(size_t)s * kLgN + k];
     }
+    if (st->steps == 0) st->steps = (int64_t)c[kJcSteps];  // batched and served jobs
     st->loss = (int64_t)c[kJcLoss];
     st->capped = (int64_t)c[kJcCapped];
     st->roulette_kills = (int64_t)c[kJcRoulette];

@@ -86,7 +86,8 @@ struct alignas(16) SourceRecF {
 // Per-job counters written by the kernel (rare events only; steps are global).
 // Rare-event counters are spread over kSlots copies (slot = block index mod kSlots) so that
 // concurrent warps do not serialise on one address; the host sums the slots.
-enum JobCounter { kJcLoss = 0, kJcCapped = 1, kJcRoulette = 2, kJcTapeEnd = 3, kJcN = 8 };
+// kJcSteps: element steps of the job's finished walks (one addition per walk)
+enum JobCounter { kJcLoss = 0, kJcCapped = 1, kJcRoulette = 2, kJcTapeEnd = 3, kJcSteps = 4, kJcN = 8 };
 enum LedgerSlot { kLgLaunched = 0, kLgAbsorbed = 1, kLgExited = 2, kLgRouletteKill = 3, kLgRouletteGain = 4, kLgLost = 5, kLgN = 8 };
 constexpr int kSlots = 64;
 

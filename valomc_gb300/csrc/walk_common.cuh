@@ -48,6 +48,9 @@ constexpr int64_t kEvTapeEnd = INT64_MIN + 4;
 template <class R> struct TraceFor { using type = NoTrace; };
 template <> struct TraceFor<TapeRng> { using type = Trace; };
 
+__device__ __forceinline__ void job_count_add(const JobDev &J, int which, unsigned long long n) {
+  atomicAdd(J.jc + (blockIdx.x & (kSlots - 1)) * kJcN + which, n);
+}
 __device__ __forceinline__ void job_count(const JobDev &J, int which) {
   atomicAdd(J.jc + (blockIdx.x & (kSlots - 1)) * kJcN + which, 1ull);
 }
