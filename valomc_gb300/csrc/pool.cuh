@@ -64,6 +64,8 @@ __global__ void __launch_bounds__(256, W::kMinBlocks) pool_kernel(const __grid_c
     if ((it & 255u) == 0u) {
       if (*reinterpret_cast<volatile const int32_t *>(&lp.ctl->cancel)) { done = true; alive = false; }
     }
+    // refill and the exit test only when some lane is idle (one vote in the common case)
+    if (__any_sync(kFull, !alive)) {
     unsigned need = __ballot_sync(kFull, !alive && !done);
     while (need) {
       if (chunk_next >= chunk_end) {
@@ -91,6 +93,7 @@ __global__ void __launch_bounds__(256, W::kMinBlocks) pool_kernel(const __grid_c
       need = __ballot_sync(kFull, !alive && !done);
     }
     if (__all_sync(kFull, done)) break;
+    }
     if (alive) {
       const int r = s.step(*J, rng, lp.max_steps);
       if (r == kScattered) { n_steps++; n_scat++; }

@@ -523,6 +523,11 @@ struct Walk3D32 {
     nsteps++;
     const float dist = fmaxf(best, 0.0f);
     const float ds = fminf(prop, dist);
+    // a photon that leaves the element: fetch the next element's optics now, so that the
+    // load runs under the deposit arithmetic
+    const int nextel = nf == 0 ? nb.x : nf == 1 ? nb.y : nf == 2 ? nb.z : nb.w;
+    float4 o2 = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (prop > dist && (unsigned)nextel < (unsigned)J.Ne) o2 = optics(J, nextel);
     px += dx * ds; py += dy * ds; pz += dz * ds;
     tr.put(el);
     const float x = mua * ds;
@@ -559,7 +564,6 @@ struct Walk3D32 {
       return res;
     }
     const float4 pf = nf == 0 ? p0 : nf == 1 ? p1 : nf == 2 ? p2 : p3;
-    const int nextel = nf == 0 ? nb.x : nf == 1 ? nb.y : nf == 2 ? nb.z : nb.w;
     if (nextel < 0) {
       const int ib = -1 - nextel;
       const uint8_t bt = __ldg(J.bctype + ib);
@@ -586,7 +590,6 @@ struct Walk3D32 {
       job_count(J, kJcLoss); job_ledger(J, kLgLost, (double)w);
       return die(J, kEvLost);
     }
-    const float4 o2 = optics(J, nextel);
     if (mus <= 0.0f && o2.y > 0.0f) {
       prop = free_path_f(unif_open_f(rng), o2.y);
       if (roulette(J, rng)) return die(J, kEvRoulette);
