@@ -487,7 +487,7 @@ struct Walk3D32 {
 
   __device__ int step(const JobDev &J, R &rng, int64_t max_steps) {
     if (rng.exhausted()) { job_count(J, kJcTapeEnd); die(J, kEvTapeEnd); return kDiedEarly; }
-    if (nsteps >= max_steps) {
+    if (nsteps >= (int32_t)min(max_steps, (int64_t)INT32_MAX)) {  // a 32-bit compare (loop invariant bound)
       job_count(J, kJcCapped); job_ledger(J, kLgLost, (double)w);
       die(J, kEvCapped);
       return kDiedEarly;
@@ -563,17 +563,22 @@ struct Walk3D32 {
       prop = free_path_f(unif_open_f(rng), mus);
       return res;
     }
-    const float4 pf = nf == 0 ? p0 : nf == 1 ? p1 : nf == 2 ? p2 : p3;
+    // the crossed face's plane, only on the (rare) mirror and Fresnel paths
+    auto face = [&]() { return nf == 0 ? p0 : nf == 1 ? p1 : nf == 2 ? p2 : p3; };
     if (nextel < 0) {
       const int ib = -1 - nextel;
       const uint8_t bt = __ldg(J.bctype + ib);
       if (is_mirror(bt)) {
+        const float4 pf = face();
         float dn = dx * pf.x + dy * pf.y + dz * pf.z;
         dx -= 2.0f * dn * pf.x; dy -= 2.0f * dn * pf.y; dz -= 2.0f * dn * pf.z;
         return kAlive;
       }
       const double bcn = __ldg(J.bcn + ib);
-      if (bcn > 0.0 && fresnel(rng, pf.x, pf.y, pf.z, (float)((double)nidx / bcn))) return kAlive;
+      if (bcn > 0.0) {
+        const float4 pf = face();
+        if (fresnel(rng, pf.x, pf.y, pf.z, (float)((double)nidx / bcn))) return kAlive;
+      }
       flush(J);
       if (!FD) add_f(J.EBR + ib, w);
       else {
@@ -593,10 +598,16 @@ struct Walk3D32 {
     if (mus <= 0.0f && o2.y > 0.0f) {
       prop = free_path_f(unif_open_f(rng), o2.y);
       if (roulette(J, rng)) return die(J, kEvRoulette);
-      if (nidx != o2.w && fresnel(rng, pf.x, pf.y, pf.z, nidx / o2.w)) return kAlive;
+      if (nidx != o2.w) {
+        const float4 pf = face();
+        if (fresnel(rng, pf.x, pf.y, pf.z, nidx / o2.w)) return kAlive;
+      }
     } else {
       if (roulette(J, rng)) return die(J, kEvRoulette);
-      if (nidx != o2.w && fresnel(rng, pf.x, pf.y, pf.z, nidx / o2.w)) return kAlive;
+      if (nidx != o2.w) {
+        const float4 pf = face();
+        if (fresnel(rng, pf.x, pf.y, pf.z, nidx / o2.w)) return kAlive;
+      }
       if (o2.y != mus) prop *= mus / o2.y;
     }
     flush(J);
