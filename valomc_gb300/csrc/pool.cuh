@@ -7,7 +7,7 @@
 // half-empty while photons remain.  A photon index selects its job (batched launches),
 // its Philox stream (key = job seed, counter = photon index) or its tape segment, and the
 // walk advances one element step per loop iteration.  Each loop iteration polls nothing
-// but registers; the host cancel flag is read every 256 iterations.
+// but registers; the host cancel flag is read every 1024 iterations.
 #pragma once
 #include "walk2d.cuh"
 
@@ -61,7 +61,7 @@ __global__ void __launch_bounds__(256, W::kMinBlocks) pool_kernel(const __grid_c
   const unsigned lt_mask = (1u << lane) - 1u;
   const long long total = lp.total;
   for (unsigned it = 0;; ++it) {
-    if ((it & 255u) == 0u) {
+    if ((it & 1023u) == 0u) {  // the host's cancel flag (an L2 round trip), every 1024 steps
       if (*reinterpret_cast<volatile const int32_t *>(&lp.ctl->cancel)) { done = true; alive = false; }
     }
     // refill and the exit test only when some lane is idle (one vote in the common case)
@@ -88,6 +88,9 @@ __global__ void __launch_bounds__(256, W::kMinBlocks) pool_kernel(const __grid_c
         start_rng(rng, *J, q);
         s.launch(*J, rng, q);
         alive = true;
+        if constexpr (W::kLaunchLoss) {
+          if (s.lost_at_launch(*J)) { alive = false; n_done++; }
+        }
       }
       chunk_next += min((long long)__popc(need), avail);
       need = __ballot_sync(kFull, !alive && !done);

@@ -26,6 +26,7 @@ __device__ __forceinline__ uint4 *philox_slot() {
 template <bool kLaunchKey>
 struct PhiloxT {
   static constexpr bool kOneJob = kLaunchKey;
+  static constexpr bool kReplay = false;
   uint32_t c0, c2;  // photon index low word, block counter
   uint4 buf;
   int32_t n;
@@ -74,6 +75,7 @@ using PhiloxOne = PhiloxT<true>;   // launch-wide key (one job)
 
 struct TapeRng {
   static constexpr bool kOneJob = false;
+  static constexpr bool kReplay = true;
   const uint32_t *p, *end;
   bool out;
   __device__ __forceinline__ void start_tape(const uint32_t *b, const uint32_t *e) { p = b; end = e; out = false; }

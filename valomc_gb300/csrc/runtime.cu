@@ -452,7 +452,7 @@ int launch_jobs(int device, const LaunchSpec &spec, const std::vector<JobDev> &j
   int status = VMC_OK;
   if (poll) {
     // The host thread watches the run: progress from the fetch counter, cancellation and
-    // the timeout set the device cancel flag, which the kernel reads every 256 steps.
+    // the timeout set the device cancel flag, which the kernel reads every 1024 steps.
     StreamGuard side;
     VMC_CK(cudaStreamCreateWithFlags(&side.s, cudaStreamNonBlocking));
     PinnedGuard pin;

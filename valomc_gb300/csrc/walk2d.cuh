@@ -26,6 +26,7 @@ template <bool FD, class R>
 struct Walk2D64 {
   static constexpr int kMinBlocks = 1;
   static constexpr bool kStaged = false;
+  static constexpr bool kLaunchLoss = false;
   Stage stage;
   using Tr = typename TraceFor<R>::type;
   double pos[2], dir[2];
@@ -300,6 +301,16 @@ struct Walk2D32 {
     return kDied;
   }
 
+  // Philox streams: a photon launched out through its own entry face is lost before its
+  // first step (as the step would find it), so the step needs no test for it
+  static constexpr bool kLaunchLoss = !R::kReplay;
+  __device__ __forceinline__ bool lost_at_launch(const JobDev &J) {
+    if (!outward) return false;
+    job_count(J, kJcLoss); job_ledger(J, kLgLost, (double)w);
+    die(J, kEvLost);
+    return true;
+  }
+
   __device__ __forceinline__ void scatter(R &rng) {
     // 2D Henyey-Greenstein: the reference's angle 2 atan(tan(-xi t pi / (g^2 - 1)) (1 - g)^2 / t)
     // with t = 1 - g^2 reduces to 2 atan(tan(pi xi) (1 - g) / (1 + g))
@@ -358,7 +369,7 @@ struct Walk2D32 {
       die(J, kEvCapped);
       return kDiedEarly;
     }
-    if (outward) {
+    if (R::kReplay && outward) {  // with Philox streams this is settled at launch
       job_count(J, kJcLoss); job_ledger(J, kLgLost, (double)w);
       die(J, kEvLost);
       return kDiedEarly;

@@ -117,6 +117,7 @@ template <bool FD, class R>
 struct Walk3D64 {
   static constexpr int kMinBlocks = 1;  // ~125 registers: 2 CTAs of 256 per SM
   static constexpr bool kStaged = false;
+  static constexpr bool kLaunchLoss = false;
   Stage stage;
   using Tr = typename TraceFor<R>::type;
   double pos[3], dir[3];
@@ -419,6 +420,16 @@ struct Walk3D32 {
     return kDied;
   }
 
+  // Philox streams: a photon launched out through its own entry face is lost before its
+  // first step (as the step would find it), so the step needs no test for it
+  static constexpr bool kLaunchLoss = !R::kReplay;
+  __device__ __forceinline__ bool lost_at_launch(const JobDev &J) {
+    if (!outward) return false;
+    job_count(J, kJcLoss); job_ledger(J, kLgLost, (double)w);
+    die(J, kEvLost);
+    return true;
+  }
+
   __device__ __forceinline__ void scatter(R &rng) {
     // Henyey-Greenstein: cos(theta) from the inverse CDF, phi uniform; same rotation as
     // ScatterPhoton (MC3D.hpp:1316-1332)
@@ -492,7 +503,7 @@ struct Walk3D32 {
       die(J, kEvCapped);
       return kDiedEarly;
     }
-    if (outward) {
+    if (R::kReplay && outward) {  // with Philox streams this is settled at launch
       job_count(J, kJcLoss); job_ledger(J, kLgLost, (double)w);
       die(J, kEvLost);
       return kDiedEarly;
