@@ -49,6 +49,11 @@ struct JobBuffers {
   int64_t *d_tape_off = nullptr, *d_trace = nullptr, *d_trace_len = nullptr;
   int64_t bytes = 0;
   int64_t Ne = 0, Nb = 0;
+  // Stream-ordered allocation (the serving loop): buffers come from `pool` on the upload
+  // stream and go back with cudaFreeAsync on `free_stream`, so that freeing a finished
+  // request never waits for the device (cudaFree would, and stall the launches in flight).
+  cudaMemPool_t pool = nullptr;
+  cudaStream_t free_stream = nullptr;
   ~JobBuffers();
   void release();
 };

@@ -76,6 +76,17 @@ static int dalloc(T **p, size_t count, int64_t &bytes) {
   return VMC_OK;
 }
 
+// from a memory pool, ordered on stream st (pool == nullptr: plain cudaMalloc)
+template <class T>
+static int dalloc(T **p, size_t count, int64_t &bytes, cudaMemPool_t pool, cudaStream_t st) {
+  if (!pool) return dalloc(p, count, bytes);
+  *p = nullptr;
+  if (count == 0) count = 1;
+  VMC_CK(cudaMallocFromPoolAsync(reinterpret_cast<void **>(p), count * sizeof(T), pool, st));
+  bytes += (int64_t)(count * sizeof(T));
+  return VMC_OK;
+}
+
 template <class T>
 static int h2d(T *d, const T *h, size_t count, cudaStream_t st) {
   if (count) VMC_CK(cudaMemcpyAsync(d, h, count * sizeof(T), cudaMemcpyHostToDevice, st));
@@ -143,7 +154,10 @@ void JobBuffers::release() {
   void *ps[] = {d_optics, d_bctype, d_bcn, d_cdf, d_src, d_cdf_f, d_src_f, d_acc, d_jc, d_ledger,
                 d_tape, d_tape_off, d_trace, d_trace_len};
   for (void *p : ps)
-    if (p) cudaFree(p);
+    if (p) {
+      if (pool) cudaFreeAsync(p, free_stream);
+      else cudaFree(p);
+    }
   d_optics = nullptr; d_bctype = nullptr; d_bcn = d_cdf = nullptr; d_src = nullptr; d_acc = nullptr;
   d_cdf_f = nullptr; d_src_f = nullptr;
   d_jc = nullptr; d_ledger = nullptr; d_tape = nullptr; d_tape_off = d_trace = d_trace_len = nullptr;
@@ -162,33 +176,33 @@ int upload_job(const HostJob &j, const DeviceMesh &m, int precision, JobBuffers 
   const size_t rows = j.homogeneous ? 1 : (size_t)Ne;
   if (precision == VMC_FP64) {
     double *d;
-    VMC_TRY(dalloc(&d, rows * 4, b.bytes));
+    VMC_TRY(dalloc(&d, rows * 4, b.bytes, b.pool, st));
     b.d_optics = d;
     VMC_TRY(h2d(d, j.optics.data(), rows * 4, st));
   } else {
     std::vector<float> f(rows * 4);
     for (size_t i = 0; i < rows * 4; i++) f[i] = (float)j.optics[i];
     float *d;
-    VMC_TRY(dalloc(&d, rows * 4, b.bytes));
+    VMC_TRY(dalloc(&d, rows * 4, b.bytes, b.pool, st));
     b.d_optics = d;
     VMC_TRY(h2d(d, f.data(), rows * 4, st));
     VMC_CK(cudaStreamSynchronize(st));  // f is a temporary
   }
-  VMC_TRY(dalloc(&b.d_bctype, (size_t)Nb, b.bytes));
+  VMC_TRY(dalloc(&b.d_bctype, (size_t)Nb, b.bytes, b.pool, st));
   VMC_TRY(h2d(b.d_bctype, j.bctype.data(), (size_t)Nb, st));
-  VMC_TRY(dalloc(&b.d_bcn, (size_t)Nb, b.bytes));
+  VMC_TRY(dalloc(&b.d_bcn, (size_t)Nb, b.bytes, b.pool, st));
   VMC_TRY(h2d(b.d_bcn, j.bcn.data(), (size_t)Nb, st));
-  VMC_TRY(dalloc(&b.d_cdf, j.cdf.size(), b.bytes));
+  VMC_TRY(dalloc(&b.d_cdf, j.cdf.size(), b.bytes, b.pool, st));
   VMC_TRY(h2d(b.d_cdf, j.cdf.data(), j.cdf.size(), st));
-  VMC_TRY(dalloc(&b.d_src, j.src.size(), b.bytes));
+  VMC_TRY(dalloc(&b.d_src, j.src.size(), b.bytes, b.pool, st));
   VMC_TRY(h2d(b.d_src, j.src.data(), j.src.size(), st));
-  VMC_TRY(dalloc(&b.d_cdf_f, j.cdf_f.size(), b.bytes));
+  VMC_TRY(dalloc(&b.d_cdf_f, j.cdf_f.size(), b.bytes, b.pool, st));
   VMC_TRY(h2d(b.d_cdf_f, j.cdf_f.data(), j.cdf_f.size(), st));
-  VMC_TRY(dalloc(&b.d_src_f, j.src_f.size(), b.bytes));
+  VMC_TRY(dalloc(&b.d_src_f, j.src_f.size(), b.bytes, b.pool, st));
   VMC_TRY(h2d(b.d_src_f, j.src_f.data(), j.src_f.size(), st));
-  VMC_TRY(dalloc(&b.d_acc, (size_t)(2 * Ne + 4 * Nb), b.bytes));
-  VMC_TRY(dalloc(&b.d_jc, (size_t)kSlots * kJcN, b.bytes));
-  VMC_TRY(dalloc(&b.d_ledger, (size_t)kSlots * kLgN, b.bytes));
+  VMC_TRY(dalloc(&b.d_acc, (size_t)(2 * Ne + 4 * Nb), b.bytes, b.pool, st));
+  VMC_TRY(dalloc(&b.d_jc, (size_t)kSlots * kJcN, b.bytes, b.pool, st));
+  VMC_TRY(dalloc(&b.d_ledger, (size_t)kSlots * kLgN, b.bytes, b.pool, st));
   return zero_job(b, st);
 }
 

@@ -77,6 +77,10 @@ struct vmc_server {
   std::condition_variable cv_collect;
   bool collector_stop = false;
   std::thread collector;
+  // request buffers: a memory pool of the device, allocated on the upload stream and
+  // returned on free_stream (no device-wide wait when a request finishes)
+  cudaMemPool_t pool = nullptr;
+  cudaStream_t free_stream = nullptr;
   void loop();
   void collect_loop();
   void finalize(Request *r);
@@ -147,6 +151,8 @@ void vmc_server::loop() {
     // them before any launch on either lane.
     for (Request *r : admitted) {
       r->buf.reset(new JobBuffers);
+      r->buf->pool = pool;
+      r->buf->free_stream = free_stream;
       DeviceMesh *m = mesh_impl(meshes[(size_t)r->mesh_id]);
       r->status = upload_job(r->job, *m, cfg.precision, *r->buf, L.st);
     }
@@ -314,6 +320,24 @@ int vmc_server_create(const vmc_server_config *cfg, vmc_server **out) {
   if (s) return s;
   vmc_server *sv = new vmc_server;
   sv->cfg = *cfg;
+  {
+    cudaMemPoolProps props;
+    memset(&props, 0, sizeof(props));
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = cfg->device;
+    cudaError_t e = cudaMemPoolCreate(&sv->pool, &props);
+    if (e == cudaSuccess) {
+      uint64_t keep = UINT64_MAX;  // keep freed blocks for the next requests
+      e = cudaMemPoolSetAttribute(sv->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sv->free_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+      if (sv->pool) cudaMemPoolDestroy(sv->pool);
+      delete sv;
+      return cuda_status(e, "server memory pool");
+    }
+  }
   sv->worker = std::thread([sv] { sv->loop(); });
   sv->collector = std::thread([sv] { sv->collect_loop(); });
   *out = sv;
@@ -416,6 +440,11 @@ int vmc_server_destroy(vmc_server *s) {
   }
   if (s->collector.joinable()) s->collector.join();
   for (auto &kv : s->all) kv.second->buf.reset();
+  if (s->free_stream) {
+    cudaStreamSynchronize(s->free_stream);
+    cudaStreamDestroy(s->free_stream);
+  }
+  if (s->pool) cudaMemPoolDestroy(s->pool);
   delete s;
   return VMC_OK;
 }
