@@ -1,5 +1,5 @@
 // tools.cu -- autotuner over launch shapes and the micro-benchmarks that give the roofline
-// denominators the photon kernels are judged against:
+// denominators the photon kernels are measured against:
 //   vmc_bench_gather: random 32-byte-sector gathers whose next address depends on the data
 //     just loaded (the shape of the element walk: load element, compute, load neighbour),
 //     over a buffer of the mesh's size, at full occupancy.  For meshes that fit in L2 this
