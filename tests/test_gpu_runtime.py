@@ -106,6 +106,22 @@ def test_server_admission_by_memory_footprint(built):
     srv.close()
 
 
+def test_server_releases_memory_of_finished_requests(built):
+    """A budget that holds one request at a time: every request is admitted in turn, so the
+    memory of finished requests (returned to the server's pool) is accounted back."""
+    p = cases()["phantom3d"][0]
+    mesh = V.Mesh(p)
+    one = V.run(p, nphoton=3000, seed=5)
+    srv = V.Server(max_slots=4, memory_budget=900_000)  # one request's state (~0.6 MB) fits, two do not
+    mid = srv.add_mesh(mesh)
+    rids = [srv.submit(mid, p, nphoton=3000, seed=5) for _ in range(6)]
+    res = [srv.wait(r, timeout_s=120) for r in rids]
+    srv.close()
+    for r in res:
+        assert r is not None and r.stats["photons_done"] == 3000
+        np.testing.assert_allclose(r.ER, one.ER, rtol=RTOL, atol=1e-300)
+
+
 def test_server_poll_before_finish(built):
     p = mg.config_3d_phantom(nphoton=1, seed=2)
     mesh = V.Mesh(p)
