@@ -329,9 +329,10 @@ def main():
         line = {
             "metric": METRIC, "value": value, "unit": "photons/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * wall_max / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 tracking, f64 accumulation",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
             "config": {"workload": WORKLOAD, "photons_per_step": nph, "precision": "fp32-track",
+                       "accumulation": "f64",
                        "l2": "flushed between steps (512 MB write)", "replicas": ws},
             "tet_steps_per_s": steps_per_launch / kmean,
             "steps_per_photon": steps_per_launch / nph,
