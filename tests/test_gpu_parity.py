@@ -158,3 +158,27 @@ def test_energy_balance_against_launched_at_full_phantom(built):
     closed = L["launched"] + L["roulette_gain"] - L["roulette_kill"]
     assert abs(L["absorbed"] + L["exited"] - closed) / L["launched"] < 1e-6
     assert abs(L["absorbed"] + L["exited"] - L["launched"]) / L["launched"] < 1e-5
+
+
+@pytest.mark.parametrize("precision,n_gpu", [(V.VMC_FP32, 1_000_000), (V.VMC_FP64, 200_000)])
+def test_fluence_within_batch_means_error_of_oracle_at_full_phantom(built, precision, n_gpu):
+    """The 648k-tet phantom itself: 20 batches of each form against 20 batches of the
+    oracle (the reference's algorithm, MT19937, all host cores) -- elements scored in every
+    batch of both agree within 3 sigma of the batch-means error."""
+    p = mg.config_3d_phantom(nphoton=1, seed=1)
+    B = 20
+    n_ref = 100_000
+    mesh = V.Mesh(p, precision=precision)
+
+    def gpu(b):
+        res, _ = V.run_batch([mesh], [p.copy(Nphoton=n_gpu, seed=3000 + b)], precision=precision)
+        return np.concatenate([res[0].ER, res[0].EBR])
+
+    def ref(b):
+        r = oracle.run(p, rng=oracle.RNG_MT, nthreads=os.cpu_count() or 1, nphoton=n_ref, seed=70000 + 1000 * b)
+        return np.concatenate([r.ER, r.EBR])
+
+    frac, chi2, nhit = compare_3sigma(batch_means(gpu, B), batch_means(ref, B))
+    assert nhit > 1000
+    assert frac >= 0.985, (precision, frac, chi2, nhit)
+    assert 0.75 < chi2 < 1.35, (precision, frac, chi2, nhit)
