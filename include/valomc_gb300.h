@@ -16,6 +16,9 @@
  *   - Every array carries its own row count so that ErrorChecks' size checks keep
  *     their codes and order.
  *   - Device memory is owned by the library (per call, or by a resident mesh handle).
+ *   - vmc_run and vmc_run_batch each run on a non-blocking stream of their own, so calls
+ *     from several host threads overlap on the GPU; a resident mesh may be shared by
+ *     concurrent calls (they only read it). vmc_run_noalloc is the exception (below).
  */
 #ifndef VALOMC_GB300_H
 #define VALOMC_GB300_H

@@ -40,6 +40,34 @@ def test_batch_equals_individual_runs(built, precision):
     assert sum(r.stats["steps"] for r in res) == tot["steps"]
 
 
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_calls_from_two_threads_overlap_and_equal_sequential_runs(built, use_graph):
+    # each call runs on a stream of its own; ctypes drops the GIL for the call
+    jobs = small_jobs()[:2]
+    opts = V.options(use_graph=use_graph)
+    seq = [V.run(p, precision=V.VMC_FP32, opts=opts) for p in jobs]
+    out = [None, None]
+    errs = []
+
+    def work(i):
+        try:
+            out[i] = [V.run(jobs[i], precision=V.VMC_FP32, opts=opts) for _ in range(3)]
+        except Exception as e:  # noqa: BLE001 -- reported below
+            errs.append(e)
+
+    th = [threading.Thread(target=work, args=(i,)) for i in range(2)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join(timeout=300)
+    assert not errs and all(o is not None for o in out)
+    for i in range(2):
+        for r in out[i]:
+            np.testing.assert_allclose(r.ER, seq[i].ER, rtol=RTOL, atol=1e-300)
+            np.testing.assert_allclose(r.DEBR, seq[i].DEBR, rtol=RTOL, atol=1e-300)
+            assert r.stats["steps"] == seq[i].stats["steps"]
+
+
 def test_batch_through_a_cuda_graph_equals_the_plain_launch(built):
     jobs = small_jobs()
     meshes = [V.Mesh(p) for p in jobs]

@@ -732,7 +732,10 @@ int vmc_run(const vmc_input *in, const vmc_options *opt_in, vmc_output *out, vmc
   if (s) return s;
   s = upload_mesh(dm, mask);
   if (s) return s;
-  cudaStream_t stream = 0;
+  // one stream per call: calls from several host threads overlap on the device
+  StreamGuard call_stream;
+  VMC_CK(cudaStreamCreateWithFlags(&call_stream.s, cudaStreamNonBlocking));
+  cudaStream_t stream = call_stream.s;
   JobBuffers jb;
   s = upload_job(hj, dm, o.precision, jb, stream);
   if (s) return s;
@@ -786,8 +789,10 @@ int vmc_run(const vmc_input *in, const vmc_options *opt_in, vmc_output *out, vmc
   s = collect_job(hj, dm, jb, in->Nphoton, o.normalize != 0 || !opt_in, out, st, stream);
   if (s) return s;
   if (ntr > 0) {
-    VMC_CK(cudaMemcpy(o.trace, jb.d_trace, sizeof(int64_t) * (size_t)(ntr * o.trace_stride), cudaMemcpyDeviceToHost));
-    VMC_CK(cudaMemcpy(o.trace_len, jb.d_trace_len, sizeof(int64_t) * (size_t)ntr, cudaMemcpyDeviceToHost));
+    VMC_CK(cudaMemcpyAsync(o.trace, jb.d_trace, sizeof(int64_t) * (size_t)(ntr * o.trace_stride),
+                           cudaMemcpyDeviceToHost, stream));
+    VMC_CK(cudaMemcpyAsync(o.trace_len, jb.d_trace_len, sizeof(int64_t) * (size_t)ntr, cudaMemcpyDeviceToHost, stream));
+    VMC_CK(cudaStreamSynchronize(stream));
   }
   auto t2 = std::chrono::steady_clock::now();
   st->seconds_setup = std::chrono::duration<double>(t1 - t0).count();
@@ -870,7 +875,9 @@ int vmc_run_batch(vmc_mesh *const *meshes, const vmc_input *jobs, int32_t njobs,
   }
   s = select_device(o.device);
   if (s) return s;
-  cudaStream_t stream = 0;
+  StreamGuard call_stream;  // one stream per call
+  VMC_CK(cudaStreamCreateWithFlags(&call_stream.s, cudaStreamNonBlocking));
+  cudaStream_t stream = call_stream.s;
   // group by launch class
   struct Group { LaunchSpec spec; std::vector<int> idx; };
   std::vector<Group> groups;
