@@ -147,9 +147,13 @@ typedef struct vmc_options {
   /* 1: record the launch (control-block reset + persistent kernel) as a CUDA graph and run
    * the instantiated graph; repeated launches of the same shape update and reuse it */
   int32_t use_graph;
-  /* > 0: each CTA stages the element-fluence deposits of up to this many elements (rounded
-   * up to a power of 2, at most 4096) in shared memory and adds them to the FP64
-   * accumulator once at its end (FP32 tetrahedral walk, continuous wave, single job) */
+  /* Shared-memory staging of the FP64 accumulators, per CTA, added to global memory once
+   * when the CTA ends.
+   * > 0: a hashed table of this many element slots (rounded up to a power of 2, at most
+   *      4096) for the element fluence (FP32 tetrahedral walk, continuous wave, single job);
+   *   0: (default) the whole accumulator set, 2 Ne + 4 Nb doubles, when the launch runs one
+   *      job, the set fits in 32 KB and the shared memory costs no resident CTA;
+   * < 0: no staging: every addition is a global reduction. */
   int32_t stage_slots;
 } vmc_options;
 

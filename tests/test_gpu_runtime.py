@@ -79,14 +79,28 @@ def test_batch_through_a_cuda_graph_equals_the_plain_launch(built):
             np.testing.assert_allclose(b.ER, a.ER, rtol=RTOL, atol=1e-300)
 
 
-@pytest.mark.parametrize("slots", [64, 2048])
-def test_shared_memory_staging_equals_global_atomics(built, slots):
-    p = cases()["phantom3d"][0].copy(Nphoton=50000, seed=31)
-    mesh = V.Mesh(p)
-    plain, _ = V.run_batch([mesh], [p], opts=V.options(stage_slots=0))
-    staged, _ = V.run_batch([mesh], [p], opts=V.options(stage_slots=slots))
-    np.testing.assert_allclose(staged[0].ER, plain[0].ER, rtol=RTOL, atol=1e-300)
-    np.testing.assert_allclose(staged[0].EBR, plain[0].EBR, rtol=RTOL, atol=1e-300)
+def staging_case(name):
+    if name == "box5":  # 750 tets, 300 boundary triangles: the whole set fits a CTA's stage
+        return mg.pencil_box(5, 0.05, 6.0, 0.9, 1.4, (2.2, 2.9), 50000, seed=31)
+    return cases()[name][0].copy(Nphoton=50000, seed=31)
+
+
+@pytest.mark.parametrize("precision", [V.VMC_FP64, V.VMC_FP32])
+@pytest.mark.parametrize("slots", [64, 2048, 0])
+@pytest.mark.parametrize("name", ["phantom3d", "box5", "square2d", "mixed2d_fd"])
+def test_shared_memory_staging_equals_global_atomics(built, slots, name, precision):
+    # slots > 0: hashed element table (3D FP32 continuous wave); 0: the whole accumulator set
+    # of a small mesh; -1: global reductions only
+    if precision == V.VMC_FP64 and slots != 0:
+        pytest.skip("the hashed table is a tracking-form option")
+    p = staging_case(name)
+    mesh = V.Mesh(p, precision=precision)
+    o = dict(precision=precision)
+    plain, _ = V.run_batch([mesh], [p], opts=V.options(stage_slots=-1, **o))
+    staged, _ = V.run_batch([mesh], [p], opts=V.options(stage_slots=slots, **o))
+    for k in ("ER", "EI", "EBR", "EBI", "DEBR", "DEBI"):
+        np.testing.assert_allclose(getattr(staged[0], k), getattr(plain[0], k), rtol=RTOL, atol=1e-300, err_msg=k)
+    assert staged[0].stats["steps"] == plain[0].stats["steps"]
 
 
 def test_autotuner_returns_a_valid_shape(built):

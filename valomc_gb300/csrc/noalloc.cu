@@ -203,7 +203,7 @@ extern "C" int vmc_run_noalloc(vmc_mesh *mesh, const vmc_input *job, const vmc_o
   lp.max_steps = o.max_steps > 0 ? o.max_steps : 10000000;
   lp.ctl = reinterpret_cast<Ctl *>(base + kOffCtl);
   lp.stage_slots = 0;
-  lp.pad = 0;
+  lp.dense = 0;
   auto t1 = std::chrono::steady_clock::now();
   if (in.Nphoton > 0) {
     void *args[] = {&lp};

@@ -34,7 +34,6 @@ __device__ __forceinline__ int find_job(const LaunchParams &lp, int64_t p) {
 // from the kernel parameters (constant bank) rather than from global memory and registers.
 template <class W, class R>
 __global__ void __launch_bounds__(256, W::kMinBlocks) pool_kernel(const __grid_constant__ LaunchParams lp) {
-  extern __shared__ __align__(16) unsigned char vmc_smem[];
   constexpr bool kOne = R::kOneJob;
   W s;
   R rng;
@@ -54,6 +53,11 @@ __global__ void __launch_bounds__(256, W::kMinBlocks) pool_kernel(const __grid_c
     }
   }
   s.stage = stg;
+  if (lp.dense > 0) {  // the CTA's copy of the single job's accumulators starts at zero
+    double *sm = reinterpret_cast<double *>(vmc_smem);
+    for (int i = threadIdx.x; i < lp.dense; i += blockDim.x) sm[i] = 0.0;
+    __syncthreads();
+  }
   bool alive = false, done = false;
   uint32_t n_steps = 0, n_scat = 0, n_done = 0;
   long long chunk_next = 0, chunk_end = 0;
@@ -118,6 +122,16 @@ __global__ void __launch_bounds__(256, W::kMinBlocks) pool_kernel(const __grid_c
         const int32_t t = stg.tag[i];
         if (t >= 0 && stg.val[i] != 0.0) atomicAdd(ER + t, stg.val[i]);
       }
+    }
+  }
+  if (lp.dense > 0) {
+    // every warp of the CTA has left the loop: add the CTA's accumulators to the job's
+    __syncthreads();
+    const double *sm = reinterpret_cast<const double *>(vmc_smem);
+    double *acc = kOne ? lp.job0.ER : lp.jobs[0].ER;
+    for (int i = threadIdx.x; i < lp.dense; i += blockDim.x) {
+      const double v = sm[i];
+      if (v != 0.0) red_global(acc + i, v);
     }
   }
   unsigned long long a = n_steps, b = n_scat, c = n_done;

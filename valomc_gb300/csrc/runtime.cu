@@ -329,7 +329,7 @@ namespace {
 struct LaunchPlan {
   const void *fn = nullptr;
   bool one = false;
-  int grid = 0, block = 0, stage_slots = 0;
+  int grid = 0, block = 0, stage_slots = 0, dense = 0;
   size_t smem = 0;
   int64_t total = 0;
   std::vector<JobDev> jobs;
@@ -363,6 +363,27 @@ int plan_launch(int device, const LaunchSpec &spec, const std::vector<JobDev> &j
   p.smem = (size_t)p.stage_slots * (sizeof(double) + sizeof(int32_t));
   VMC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, p.fn, p.block, p.smem));
   if (per_sm < 1) { set_error("kernel does not fit on an SM at this block size"); return VMC_ERR_INVALID_ARGUMENT; }
+  // A single job on a small mesh, without the hashed stage: every CTA keeps the whole
+  // accumulator set (2 Ne + 4 Nb doubles) in shared memory, when that costs no resident
+  // CTA, and adds it to the job's accumulators once at its end (stage_slots < 0: off).
+  p.dense = 0;
+  if (spec.stage_slots >= 0 && p.stage_slots == 0 && p.jobs.size() == 1) {
+    JobDev &j = p.jobs[0];
+    const int64_t Ne = j.Ne, Nb = j.Nb, n = 2 * Ne + 4 * Nb;
+    const bool packed = j.EI == j.ER + Ne && j.EBR == j.ER + 2 * Ne && j.EBI == j.EBR + Nb &&
+                        j.DEBR == j.EBR + 2 * Nb && j.DEBI == j.EBR + 3 * Nb;
+    if (packed && n > 0 && n * (int64_t)sizeof(double) <= kDenseStageBytes) {
+      int per_sm_dense = 0;
+      VMC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_dense, p.fn, p.block, (size_t)n * sizeof(double)));
+      const int want = spec.blocks_per_sm > 0 ? std::min(per_sm, spec.blocks_per_sm) : per_sm;
+      if (per_sm_dense >= want) {
+        p.dense = (int)n;
+        j.dense = (int32_t)n;
+        p.smem = (size_t)n * sizeof(double);
+        per_sm = per_sm_dense;
+      }
+    }
+  }
   if (spec.blocks_per_sm > 0) per_sm = std::min(per_sm, spec.blocks_per_sm);
   p.grid = per_sm * sms;
   res.grid = p.grid;
@@ -382,7 +403,7 @@ LaunchParams make_params(const LaunchSpec &spec, const LaunchPlan &p, const JobD
   lp.max_steps = spec.max_steps > 0 ? spec.max_steps : 10000000;
   lp.ctl = dctl;
   lp.stage_slots = p.stage_slots;
-  lp.pad = 0;
+  lp.dense = p.dense;
   return lp;
 }
 

@@ -90,6 +90,8 @@ struct alignas(16) SourceRecF {
 enum JobCounter { kJcLoss = 0, kJcCapped = 1, kJcRoulette = 2, kJcTapeEnd = 3, kJcSteps = 4, kJcN = 8 };
 enum LedgerSlot { kLgLaunched = 0, kLgAbsorbed = 1, kLgExited = 2, kLgRouletteKill = 3, kLgRouletteGain = 4, kLgLost = 5, kLgN = 8 };
 constexpr int kSlots = 64;
+// largest accumulator set (2 Ne + 4 Nb doubles) a launch stages whole in each CTA's shared memory
+constexpr int64_t kDenseStageBytes = 32 * 1024;
 
 struct JobDev {
   const void *geom;            // Tet64 / Tet32 / Tri64 / Tri32 [Ne]
@@ -107,7 +109,7 @@ struct JobDev {
   double omega;                // 2 pi f
   double k_scale;              // omega / c0: k = k_scale * n  (cpp/3d/MC3D.hpp:662)
   float k_scale_f;             // the same in FP32, for the tracking form
-  float pad_k;
+  int32_t dense;               // > 0: the launch stages the 2 Ne + 4 Nb accumulators per CTA in shared memory
   double phase0;
   uint64_t seed;
   uint32_t stream;
@@ -143,7 +145,7 @@ struct LaunchParams {
   int64_t max_steps;
   Ctl *ctl;
   int32_t stage_slots;        // > 0: per-CTA shared-memory staging of ER deposits (power of 2)
-  int32_t pad;
+  int32_t dense;              // > 0: doubles of the single job's accumulators staged per CTA (as JobDev::dense)
   // launches of one job (the kernels whose RNG has kOneJob): the job's descriptor and the
   // ten Philox round keys of its seed, (lo, hi) per round
   JobDev job0;

@@ -56,8 +56,8 @@ struct Walk2D64 {
   }
 
   __device__ __forceinline__ void flush(const JobDev &J) {
-    add_d(J.ER + el, acc);
-    if (FD) add_d(J.EI + el, accI);
+    add_d(J, J.ER + el, acc);
+    if (FD) add_d(J, J.EI + el, accI);
     acc = accI = 0.0;
   }
 
@@ -197,13 +197,13 @@ struct Walk2D64 {
       double dn = dir[0] * nor[0] + dir[1] * nor[1];
       flush(J);
       if (!FD) {
-        add_d(J.EBR + ib, w);
-        add_d(J.DEBR + ib, w / dn);
+        add_d(J, J.EBR + ib, w);
+        add_d(J, J.DEBR + ib, w / dn);
       } else {
-        add_d(J.EBR + ib, w * cph);
-        add_d(J.EBI + ib, -(w * sph));
-        add_d(J.DEBR + ib, w * cph / dn);
-        add_d(J.DEBI + ib, -(w * sph / dn));
+        add_d(J, J.EBR + ib, w * cph);
+        add_d(J, J.EBI + ib, -(w * sph));
+        add_d(J, J.DEBR + ib, w * cph / dn);
+        add_d(J, J.DEBI + ib, -(w * sph / dn));
       }
       tr.put(-1 - (int64_t)ib);
       tr.end();
@@ -280,7 +280,7 @@ struct Walk2D32 {
       outward = ln.x * dx + ln.y * dy > 0.0f;
     }
     w = 1.0f;
-    phase = fmodf((float)J.phase0, kTwoPiF);
+    phase = fmodf(d2f_int(J.phase0), kTwoPiF);
     float4 o = optics(J, el);
     mua = o.x; mus = o.y; g = o.z; nidx = o.w;
     prop = free_path_f(unif_open_f(rng), mus);
@@ -289,8 +289,8 @@ struct Walk2D32 {
   }
 
   __device__ __forceinline__ void flush(const JobDev &J) {
-    add_f(J.ER + el, acc);
-    if (FD) add_f(J.EI + el, accI);
+    add_f(J, J.ER + el, acc);
+    if (FD) add_f(J, J.EI + el, accI);
     acc = accI = 0.0f;
   }
 
@@ -306,7 +306,7 @@ struct Walk2D32 {
   static constexpr bool kLaunchLoss = !R::kReplay;
   __device__ __forceinline__ bool lost_at_launch(const JobDev &J) {
     if (!outward) return false;
-    job_count(J, kJcLoss); job_ledger(J, kLgLost, (double)w);
+    job_count(J, kJcLoss); job_ledger(J, kLgLost, f2d_int(w));
     die(J, kEvLost);
     return true;
   }
@@ -347,11 +347,11 @@ struct Walk2D32 {
   __device__ __forceinline__ bool roulette(const JobDev &J, R &rng) {
     if (w < (float)kWeight0) {
       if (unif_closed_f(rng) > (float)kChance) {
-        job_count(J, kJcRoulette); job_ledger(J, kLgRouletteKill, (double)w);
+        job_count(J, kJcRoulette); job_ledger(J, kLgRouletteKill, f2d_int(w));
         return true;
       }
       float nw = w * 10.0f;
-      job_ledger(J, kLgRouletteGain, (double)nw - (double)w);
+      job_ledger(J, kLgRouletteGain, f2d_int(nw) - f2d_int(w));
       w = nw;
     }
     return false;
@@ -365,12 +365,12 @@ struct Walk2D32 {
   __device__ int step(const JobDev &J, R &rng, int64_t max_steps) {
     if (rng.exhausted()) { job_count(J, kJcTapeEnd); die(J, kEvTapeEnd); return kDiedEarly; }
     if (nsteps >= max_steps) {
-      job_count(J, kJcCapped); job_ledger(J, kLgLost, (double)w);
+      job_count(J, kJcCapped); job_ledger(J, kLgLost, f2d_int(w));
       die(J, kEvCapped);
       return kDiedEarly;
     }
     if (R::kReplay && outward) {  // with Philox streams this is settled at launch
-      job_count(J, kJcLoss); job_ledger(J, kLgLost, (double)w);
+      job_count(J, kJcLoss); job_ledger(J, kLgLost, f2d_int(w));
       die(J, kEvLost);
       return kDiedEarly;
     }
@@ -392,7 +392,7 @@ struct Walk2D32 {
       }
     }
     if (nf < 0) {
-      job_count(J, kJcLoss); job_ledger(J, kLgLost, (double)w);
+      job_count(J, kJcLoss); job_ledger(J, kLgLost, f2d_int(w));
       die(J, kEvLost);
       return kDiedEarly;
     }
@@ -442,27 +442,27 @@ struct Walk2D32 {
         dx -= 2.0f * dn * nx; dy -= 2.0f * dn * ny;
         return kAlive;
       }
-      const double bcn = __ldg(J.bcn + ib);
-      if (bcn > 0.0 && fresnel(rng, nx, ny, (float)((double)nidx / bcn), true)) return kAlive;
+      const float bcn = d2f_int(__ldg(J.bcn + ib));
+      if (bcn > 0.0f && fresnel(rng, nx, ny, nidx / bcn, true)) return kAlive;
       float dn = dx * nx + dy * ny;
       flush(J);
       if (!FD) {
-        add_f(J.EBR + ib, w);
-        add_f(J.DEBR + ib, __fdividef(w, dn));
+        add_f(J, J.EBR + ib, w);
+        add_f(J, J.DEBR + ib, __fdividef(w, dn));
       } else {
         float sp, cp;
         sincosf(phase, &sp, &cp);
-        add_f(J.EBR + ib, w * cp);
-        add_f(J.EBI + ib, -(w * sp));
-        add_f(J.DEBR + ib, __fdividef(w * cp, dn));
-        add_f(J.DEBI + ib, -__fdividef(w * sp, dn));
+        add_f(J, J.EBR + ib, w * cp);
+        add_f(J, J.EBI + ib, -(w * sp));
+        add_f(J, J.DEBR + ib, __fdividef(w * cp, dn));
+        add_f(J, J.DEBI + ib, -__fdividef(w * sp, dn));
       }
       tr.put(-1 - (int64_t)ib);
       tr.end();
       return kDied;
     }
     if (nextel >= J.Ne) {
-      job_count(J, kJcLoss); job_ledger(J, kLgLost, (double)w);
+      job_count(J, kJcLoss); job_ledger(J, kLgLost, f2d_int(w));
       return die(J, kEvLost);
     }
     const float4 o2 = optics(J, nextel);

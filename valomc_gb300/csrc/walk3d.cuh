@@ -147,8 +147,8 @@ struct Walk3D64 {
   }
 
   __device__ __forceinline__ void flush(const JobDev &J) {
-    add_d(J.ER + el, acc);
-    if (FD) add_d(J.EI + el, accI);
+    add_d(J, J.ER + el, acc);
+    if (FD) add_d(J, J.EI + el, accI);
     acc = accI = 0.0;
   }
 
@@ -288,8 +288,8 @@ struct Walk3D64 {
         if (fresnel(rng, nor, nidx / bcn, nf)) return kAlive;
       }
       flush(J);
-      if (!FD) add_d(J.EBR + ib, w);
-      else { add_d(J.EBR + ib, w * cph); add_d(J.EBI + ib, -(w * sph)); }
+      if (!FD) add_d(J, J.EBR + ib, w);
+      else { add_d(J, J.EBR + ib, w * cph); add_d(J, J.EBI + ib, -(w * sph)); }
       tr.put(-1 - (int64_t)ib);
       tr.end();
       return kDied;
@@ -398,7 +398,7 @@ struct Walk3D32 {
       outward = pl.x * dx + pl.y * dy + pl.z * dz > 0.0f;
     }
     w = 1.0f;
-    phase = fmodf((float)J.phase0, kTwoPiF);
+    phase = fmodf(d2f_int(J.phase0), kTwoPiF);
     float4 o = optics(J, el);
     mua = o.x; mus = o.y; g = o.z; nidx = o.w;
     prop = free_path_f(unif_open_f(rng), mus);
@@ -407,9 +407,9 @@ struct Walk3D32 {
   }
 
   __device__ __forceinline__ void flush(const JobDev &J) {
-    if (!FD) add_staged(stage, J.ER, el, acc);
-    else add_f(J.ER + el, acc);
-    if (FD) add_f(J.EI + el, accI);
+    if (!FD) add_staged(stage, J, el, acc);
+    else add_f(J, J.ER + el, acc);
+    if (FD) add_f(J, J.EI + el, accI);
     acc = accI = 0.0f;
   }
 
@@ -425,7 +425,7 @@ struct Walk3D32 {
   static constexpr bool kLaunchLoss = !R::kReplay;
   __device__ __forceinline__ bool lost_at_launch(const JobDev &J) {
     if (!outward) return false;
-    job_count(J, kJcLoss); job_ledger(J, kLgLost, (double)w);
+    job_count(J, kJcLoss); job_ledger(J, kLgLost, f2d_int(w));
     die(J, kEvLost);
     return true;
   }
@@ -486,11 +486,11 @@ struct Walk3D32 {
   __device__ __forceinline__ bool roulette(const JobDev &J, R &rng) {
     if (w < (float)kWeight0) {
       if (unif_closed_f(rng) > (float)kChance) {
-        job_count(J, kJcRoulette); job_ledger(J, kLgRouletteKill, (double)w);
+        job_count(J, kJcRoulette); job_ledger(J, kLgRouletteKill, f2d_int(w));
         return true;
       }
       float nw = w * 10.0f;
-      job_ledger(J, kLgRouletteGain, (double)nw - (double)w);
+      job_ledger(J, kLgRouletteGain, f2d_int(nw) - f2d_int(w));
       w = nw;
     }
     return false;
@@ -499,12 +499,12 @@ struct Walk3D32 {
   __device__ int step(const JobDev &J, R &rng, int64_t max_steps) {
     if (rng.exhausted()) { job_count(J, kJcTapeEnd); die(J, kEvTapeEnd); return kDiedEarly; }
     if (nsteps >= (int32_t)min(max_steps, (int64_t)INT32_MAX)) {  // a 32-bit compare (loop invariant bound)
-      job_count(J, kJcCapped); job_ledger(J, kLgLost, (double)w);
+      job_count(J, kJcCapped); job_ledger(J, kLgLost, f2d_int(w));
       die(J, kEvCapped);
       return kDiedEarly;
     }
     if (R::kReplay && outward) {  // with Philox streams this is settled at launch
-      job_count(J, kJcLoss); job_ledger(J, kLgLost, (double)w);
+      job_count(J, kJcLoss); job_ledger(J, kLgLost, f2d_int(w));
       die(J, kEvLost);
       return kDiedEarly;
     }
@@ -527,7 +527,7 @@ struct Walk3D32 {
       }
     }
     if (nf < 0) {
-      job_count(J, kJcLoss); job_ledger(J, kLgLost, (double)w);
+      job_count(J, kJcLoss); job_ledger(J, kLgLost, f2d_int(w));
       die(J, kEvLost);
       return kDiedEarly;
     }
@@ -585,25 +585,25 @@ struct Walk3D32 {
         dx -= 2.0f * dn * pf.x; dy -= 2.0f * dn * pf.y; dz -= 2.0f * dn * pf.z;
         return kAlive;
       }
-      const double bcn = __ldg(J.bcn + ib);
-      if (bcn > 0.0) {
+      const float bcn = d2f_int(__ldg(J.bcn + ib));
+      if (bcn > 0.0f) {
         const float4 pf = face();
-        if (fresnel(rng, pf.x, pf.y, pf.z, (float)((double)nidx / bcn))) return kAlive;
+        if (fresnel(rng, pf.x, pf.y, pf.z, nidx / bcn)) return kAlive;
       }
       flush(J);
-      if (!FD) add_f(J.EBR + ib, w);
+      if (!FD) add_f(J, J.EBR + ib, w);
       else {
         float sp, cp;
         sincosf(phase, &sp, &cp);
-        add_f(J.EBR + ib, w * cp);
-        add_f(J.EBI + ib, -(w * sp));
+        add_f(J, J.EBR + ib, w * cp);
+        add_f(J, J.EBI + ib, -(w * sp));
       }
       tr.put(-1 - (int64_t)ib);
       tr.end();
       return kDied;
     }
     if (nextel >= J.Ne) {
-      job_count(J, kJcLoss); job_ledger(J, kLgLost, (double)w);
+      job_count(J, kJcLoss); job_ledger(J, kLgLost, f2d_int(w));
       return die(J, kEvLost);
     }
     if (mus <= 0.0f && o2.y > 0.0f) {

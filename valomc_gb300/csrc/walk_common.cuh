@@ -164,8 +164,26 @@ __device__ __forceinline__ void red_global(double *p, double v) {
   asm volatile("red.global.add.f64 [%0], %1;" :: "l"(__cvta_generic_to_global(p)), "d"(v));
 }
 
-__device__ __forceinline__ void add_d(double *p, double v) {
-  if (v != 0.0) red_global(p, v);
+// The pool kernel's dynamic shared memory (every extern __shared__ array names this base).
+extern __shared__ __align__(16) unsigned char vmc_smem[];
+
+__device__ __forceinline__ void red_shared(double *p, double v) {
+  asm volatile("red.shared.add.f64 [%0], %1;" :: "r"((uint32_t)__cvta_generic_to_shared(p)), "d"(v));
+}
+
+// Addition into one of the job's FP64 accumulators (ER, EI, EBR, EBI, DEBR, DEBI, back to
+// back from ER).  When the launch stages the whole set in each CTA's shared memory
+// (J.dense > 0: one job on a small mesh) the addition stays in the CTA and the kernel adds
+// the CTA's copy to global memory once at its end; otherwise it is a global reduction.  On
+// a mesh of a few hundred elements the global reductions all land in a handful of L2 lines,
+// whose slice's atomic unit then limits the whole launch.
+__device__ __forceinline__ void acc_add(const JobDev &J, double *p, double v) {
+  if (J.dense) red_shared(reinterpret_cast<double *>(vmc_smem) + (p - J.ER), v);
+  else red_global(p, v);
+}
+
+__device__ __forceinline__ void add_d(const JobDev &J, double *p, double v) {
+  if (v != 0.0) acc_add(J, p, v);
 }
 
 // float -> double by bit manipulation on the integer pipe (exact for normal floats; zero
@@ -180,13 +198,27 @@ __device__ __forceinline__ double f2d_int(float x) {
   return __longlong_as_double((long long)bits);
 }
 
-__device__ __forceinline__ void add_f(double *p, float v) {
-  if (v != 0.0f) red_global(p, f2d_int(v));
+// double -> float, rounded to nearest even, on the integer pipe for zeros and doubles in
+// float's normal range (anything else through the FP64 pipe's conversion)
+__device__ __forceinline__ float d2f_int(double x) {
+  const uint64_t b = (uint64_t)__double_as_longlong(x);
+  if ((b << 1) == 0u) return __uint_as_float((uint32_t)(b >> 32));
+  const int e = (int)((b >> 52) & 0x7ffu) - 1023 + 127;
+  if (e <= 0 || e >= 255) return (float)x;
+  const uint32_t m = (uint32_t)(b >> 29) & 0x7fffffu;
+  const uint32_t rest = (uint32_t)b & 0x1fffffffu;
+  uint32_t r = ((uint32_t)(b >> 63) << 31) | ((uint32_t)e << 23) | m;
+  if (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) r += 1u;  // a carry moves into the exponent
+  return __uint_as_float(r);
+}
+
+__device__ __forceinline__ void add_f(const JobDev &J, double *p, float v) {
+  if (v != 0.0f) acc_add(J, p, f2d_int(v));
 }
 
 // element deposit through the CTA's shared-memory stage when it holds (or can claim) the
 // element's slot, else straight to the global accumulator
-__device__ __forceinline__ void add_staged(const Stage &S, double *ER, int el, float v) {
+__device__ __forceinline__ void add_staged(const Stage &S, const JobDev &J, int el, float v) {
   if (v == 0.0f) return;
   const double d = f2d_int(v);
   if (S.mask) {
@@ -198,7 +230,7 @@ __device__ __forceinline__ void add_staged(const Stage &S, double *ER, int el, f
       return;
     }
   }
-  red_global(ER + el, d);
+  acc_add(J, J.ER + el, d);
 }
 
 // ---- FP32 launch for the tracking form: same draws and sampling laws as CreatePhoton,
