@@ -155,6 +155,9 @@ typedef struct vmc_options {
    *      job, the set fits in 32 KB and the shared memory costs no resident CTA;
    * < 0: no staging: every addition is a global reduction. */
   int32_t stage_slots;
+  /* a warp relaunches its idle lanes once at least this many are idle, or on every 8th
+   * loop iteration, so that short walks launch their photons together; 0 = default */
+  int32_t refill_lanes;
 } vmc_options;
 
 typedef struct vmc_stats {

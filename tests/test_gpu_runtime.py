@@ -103,6 +103,19 @@ def test_shared_memory_staging_equals_global_atomics(built, slots, name, precisi
     assert staged[0].stats["steps"] == plain[0].stats["steps"]
 
 
+@pytest.mark.parametrize("name", ["square2d", "phantom3d"])
+def test_refill_threshold_leaves_results_unchanged(built, name):
+    # a photon's draws depend on its index only, so launching idle lanes one at a time or in
+    # groups changes nothing but the order of the FP64 additions
+    p = cases()[name][0].copy(Nphoton=40000, seed=41)
+    ref = V.run(p, opts=V.options(refill_lanes=1))
+    for k in (4, 32):
+        r = V.run(p, opts=V.options(refill_lanes=k))
+        np.testing.assert_allclose(r.ER, ref.ER, rtol=RTOL, atol=1e-300)
+        np.testing.assert_allclose(r.EBR, ref.EBR, rtol=RTOL, atol=1e-300)
+        assert r.stats["steps"] == ref.stats["steps"] and r.stats["photons_done"] == p.Nphoton
+
+
 def test_autotuner_returns_a_valid_shape(built):
     jobs = small_jobs()
     meshes = [V.Mesh(p) for p in jobs]

@@ -80,6 +80,7 @@ class VmcOptions(C.Structure):
         ("tape", C.POINTER(C.c_uint32)), ("tape_off", _p64), ("tape_photons", C.c_int64),
         ("trace", _p64), ("trace_len", _p64), ("trace_stride", C.c_int64), ("trace_photons", C.c_int64),
         ("photon_offset", C.c_int64), ("use_graph", C.c_int32), ("stage_slots", C.c_int32),
+        ("refill_lanes", C.c_int32),
     ]
 
 
@@ -251,10 +252,11 @@ def _outputs(Ne, Nb, dim, want_hn):
 
 def options(precision=VMC_FP32, device=0, block_size=0, blocks_per_sm=0, fetch_chunk=0, max_steps=0,
             timeout_s=0.0, stream_id=0, normalize=True, progress=None, cancel=None, photon_offset=0, use_graph=False,
-            stage_slots=None):
+            stage_slots=None, refill_lanes=0):
     o = VmcOptions()
     lib().vmc_default_options(C.byref(o))
     o.use_graph = int(bool(use_graph))
+    o.refill_lanes = int(refill_lanes)
     if stage_slots is not None:
         o.stage_slots = int(stage_slots)
     o.precision, o.device = precision, device

@@ -69,6 +69,7 @@ struct LaunchSpec {
   bool graph = false;  // launch through a (reused) CUDA graph
   int stage_slots = 0; // shared-memory staging slots per CTA (0: off)
   int block = 0, blocks_per_sm = 0, chunk = 0;
+  int refill = 0;      // idle lanes a warp waits for before relaunching (0: default)
   int64_t max_steps = 0;
 };
 struct LaunchResult {

@@ -526,6 +526,7 @@ int build_job(const vmc_input *in, const HostMesh &m, HostJob &j) {
       F.n[c] = (float)S.n[c]; F.e1[c] = (float)S.e1[c]; F.e2[c] = (float)S.e2[c]; F.L[c] = (float)S.L[c];
     }
     F.phi0 = (float)S.phi0; F.sigma = (float)S.sigma; F.gauss_h = (float)S.gauss_h;
+    F.cphi0 = (float)cos(S.phi0); F.sphi0 = (float)sin(S.phi0);
     F.mother = S.mother; F.curface = S.curface; F.ib = S.ib; F.type = S.type; F.dirtype = S.dirtype;
     j.cdf_f[i] = (float)j.cdf[i];
   }

@@ -204,6 +204,7 @@ extern "C" int vmc_run_noalloc(vmc_mesh *mesh, const vmc_input *job, const vmc_o
   lp.ctl = reinterpret_cast<Ctl *>(base + kOffCtl);
   lp.stage_slots = 0;
   lp.dense = 0;
+  lp.refill_min = o.refill_lanes > 0 ? o.refill_lanes : kDefaultRefill;
   auto t1 = std::chrono::steady_clock::now();
   if (in.Nphoton > 0) {
     void *args[] = {&lp};

@@ -71,6 +71,8 @@ __global__ void __launch_bounds__(256, W::kMinBlocks) pool_kernel(const __grid_c
     // refill and the exit test only when some lane is idle (one vote in the common case)
     if (__any_sync(kFull, !alive)) {
     unsigned need = __ballot_sync(kFull, !alive && !done);
+    // short walks: wait (at most 7 iterations) until enough lanes are idle to launch together
+    if (__popc(need) < lp.refill_min && (it & 7u) != 0u) need = 0u;
     while (need) {
       if (chunk_next >= chunk_end) {
         unsigned long long base = 0;

@@ -404,6 +404,7 @@ LaunchParams make_params(const LaunchSpec &spec, const LaunchPlan &p, const JobD
   lp.ctl = dctl;
   lp.stage_slots = p.stage_slots;
   lp.dense = p.dense;
+  lp.refill_min = spec.refill > 0 ? spec.refill : kDefaultRefill;
   return lp;
 }
 
@@ -796,6 +797,7 @@ int vmc_run(const vmc_input *in, const vmc_options *opt_in, vmc_output *out, vmc
   spec.max_steps = o.max_steps;
   spec.graph = o.use_graph != 0;
   spec.stage_slots = o.stage_slots;
+  spec.refill = o.refill_lanes;
   LaunchResult lr;
   int ls = launch_jobs(o.device, spec, std::vector<JobDev>{d}, &o, stream, lr);
   if (ls != VMC_OK && ls != VMC_ERR_CANCELLED && ls != VMC_ERR_TIMEOUT) return ls;
@@ -913,6 +915,7 @@ int vmc_run_batch(vmc_mesh *const *meshes, const vmc_input *jobs, int32_t njobs,
     sp.max_steps = o.max_steps;
     sp.graph = o.use_graph != 0;
     sp.stage_slots = o.stage_slots;
+    sp.refill = o.refill_lanes;
     auto it = std::find_if(groups.begin(), groups.end(), [&](const Group &g) { return g.spec.dim == sp.dim && g.spec.fd == sp.fd; });
     if (it == groups.end()) { groups.push_back(Group{sp, {}}); it = groups.end() - 1; }
     it->idx.push_back(i);

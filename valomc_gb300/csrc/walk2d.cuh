@@ -317,10 +317,16 @@ struct Walk2D32 {
     float xi = unif_halfup_f(rng);
     float sn, cs;
     if (g != 0.0f) {
+      // th = 2 atan(z), z = k tan(pi xi), k = (1 - g) / (1 + g): with (s0, c0) the sine and
+      // cosine of pi xi, cos th = (c0^2 - (k s0)^2) / (c0^2 + (k s0)^2) and
+      // sin th = 2 k s0 c0 / (c0^2 + (k s0)^2) -- no arctangent, no sine of th
       float s0, c0;
       sincospif(xi, &s0, &c0);
-      float th = 2.0f * atanf(s0 * ((1.0f - g) / (1.0f + g)) / c0);
-      sincosf(th, &sn, &cs);
+      const float ks = __fdividef(1.0f - g, 1.0f + g) * s0;
+      const float a = c0 * c0, b = ks * ks;
+      const float inv = __fdividef(1.0f, a + b);
+      cs = (a - b) * inv;
+      sn = 2.0f * ks * c0 * inv;
       float nx = dx * cs - dy * sn, ny = dx * sn + dy * cs;
       float in = rsqrtf(nx * nx + ny * ny);
       dx = nx * in; dy = ny * in;

@@ -313,12 +313,22 @@ __device__ __forceinline__ void create_photon_2d_f(const JobDev &J, R &rng, floa
   if (bt == 'l') {
     if (dt != 'n') { dir[0] = S.L[0]; dir[1] = S.L[1]; }
   } else if (bt == 'i') {
-    const float phi = (float)kPi * (unif_open_f(rng) - 0.5f);
-    sincosf(S.phi0 + phi, &dir[1], &dir[0]);
+    // the direction at phi0 + phi, as (cos phi0, sin phi0) turned by phi
+    float sp, cp;
+    sincospif(unif_open_f(rng) - 0.5f, &sp, &cp);
+    dir[0] = S.cphi0 * cp - S.sphi0 * sp;
+    dir[1] = S.sphi0 * cp + S.cphi0 * sp;
   } else if (bt == 'c' || bt == 'g') {
     for (int it = 0; it < kMaxRejections; it++) {
-      const float phi = (bt == 'c') ? asinf(2.0f * unif_open_f(rng) - 1.0f) : gauss_angle_f(rng, S.sigma, S.gauss_h);
-      sincosf(S.phi0 + phi, &dir[1], &dir[0]);
+      float sp, cp;
+      if (bt == 'c') {  // phi = asin(s): sin phi = s, cos phi = sqrt(1 - s^2)
+        sp = 2.0f * unif_open_f(rng) - 1.0f;
+        cp = sqrtf(fmaxf(0.0f, 1.0f - sp * sp));
+      } else {
+        sincosf(gauss_angle_f(rng, S.sigma, S.gauss_h), &sp, &cp);
+      }
+      dir[0] = S.cphi0 * cp - S.sphi0 * sp;
+      dir[1] = S.sphi0 * cp + S.cphi0 * sp;
       if (dt == 'n' || n0 * dir[0] + n1 * dir[1] > 0.0f || rng.exhausted()) break;
     }
   }
