@@ -340,7 +340,8 @@ int plan_launch(int device, const LaunchSpec &spec, const std::vector<JobDev> &j
                 LaunchResult &res) {
   int sms = 0;
   VMC_TRY(select_device(device, &sms));
-  p.one = jobs_in.size() == 1 && !spec.tape;
+  // the one-job kernels: FP32 walks on Philox streams (descriptor and keys as parameters)
+  p.one = jobs_in.size() == 1 && !spec.tape && spec.precision == VMC_FP32;
   p.fn = select_kernel(spec, p.one);
   if (!p.fn) { set_error("no kernel for this configuration"); return VMC_ERR_INVALID_ARGUMENT; }
   p.jobs = jobs_in;
@@ -363,11 +364,11 @@ int plan_launch(int device, const LaunchSpec &spec, const std::vector<JobDev> &j
   p.smem = (size_t)p.stage_slots * (sizeof(double) + sizeof(int32_t));
   VMC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, p.fn, p.block, p.smem));
   if (per_sm < 1) { set_error("kernel does not fit on an SM at this block size"); return VMC_ERR_INVALID_ARGUMENT; }
-  // A single job on a small mesh, without the hashed stage: every CTA keeps the whole
+  // A one-job launch on a small mesh, without the hashed stage: every CTA keeps the whole
   // accumulator set (2 Ne + 4 Nb doubles) in shared memory, when that costs no resident
   // CTA, and adds it to the job's accumulators once at its end (stage_slots < 0: off).
   p.dense = 0;
-  if (spec.stage_slots >= 0 && p.stage_slots == 0 && p.jobs.size() == 1) {
+  if (spec.stage_slots >= 0 && p.stage_slots == 0 && p.one) {
     JobDev &j = p.jobs[0];
     const int64_t Ne = j.Ne, Nb = j.Nb, n = 2 * Ne + 4 * Nb;
     const bool packed = j.EI == j.ER + Ne && j.EBR == j.ER + 2 * Ne && j.EBI == j.EBR + Nb &&

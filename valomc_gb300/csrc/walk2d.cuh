@@ -289,8 +289,8 @@ struct Walk2D32 {
   }
 
   __device__ __forceinline__ void flush(const JobDev &J) {
-    add_f(J, J.ER + el, acc);
-    if (FD) add_f(J, J.EI + el, accI);
+    add_f<R::kOneJob>(J, J.ER + el, acc);
+    if (FD) add_f<R::kOneJob>(J, J.EI + el, accI);
     acc = accI = 0.0f;
   }
 
@@ -453,15 +453,15 @@ struct Walk2D32 {
       float dn = dx * nx + dy * ny;
       flush(J);
       if (!FD) {
-        add_f(J, J.EBR + ib, w);
-        add_f(J, J.DEBR + ib, __fdividef(w, dn));
+        add_f<R::kOneJob>(J, J.EBR + ib, w);
+        add_f<R::kOneJob>(J, J.DEBR + ib, __fdividef(w, dn));
       } else {
         float sp, cp;
         sincosf(phase, &sp, &cp);
-        add_f(J, J.EBR + ib, w * cp);
-        add_f(J, J.EBI + ib, -(w * sp));
-        add_f(J, J.DEBR + ib, __fdividef(w * cp, dn));
-        add_f(J, J.DEBI + ib, -__fdividef(w * sp, dn));
+        add_f<R::kOneJob>(J, J.EBR + ib, w * cp);
+        add_f<R::kOneJob>(J, J.EBI + ib, -(w * sp));
+        add_f<R::kOneJob>(J, J.DEBR + ib, __fdividef(w * cp, dn));
+        add_f<R::kOneJob>(J, J.DEBI + ib, -__fdividef(w * sp, dn));
       }
       tr.put(-1 - (int64_t)ib);
       tr.end();

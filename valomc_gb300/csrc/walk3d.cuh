@@ -407,9 +407,9 @@ struct Walk3D32 {
   }
 
   __device__ __forceinline__ void flush(const JobDev &J) {
-    if (!FD) add_staged(stage, J, el, acc);
-    else add_f(J, J.ER + el, acc);
-    if (FD) add_f(J, J.EI + el, accI);
+    if (!FD) add_staged<R::kOneJob>(stage, J, el, acc);
+    else add_f<R::kOneJob>(J, J.ER + el, acc);
+    if (FD) add_f<R::kOneJob>(J, J.EI + el, accI);
     acc = accI = 0.0f;
   }
 
@@ -591,12 +591,12 @@ struct Walk3D32 {
         if (fresnel(rng, pf.x, pf.y, pf.z, nidx / bcn)) return kAlive;
       }
       flush(J);
-      if (!FD) add_f(J, J.EBR + ib, w);
+      if (!FD) add_f<R::kOneJob>(J, J.EBR + ib, w);
       else {
         float sp, cp;
         sincosf(phase, &sp, &cp);
-        add_f(J, J.EBR + ib, w * cp);
-        add_f(J, J.EBI + ib, -(w * sp));
+        add_f<R::kOneJob>(J, J.EBR + ib, w * cp);
+        add_f<R::kOneJob>(J, J.EBI + ib, -(w * sp));
       }
       tr.put(-1 - (int64_t)ib);
       tr.end();

@@ -173,17 +173,24 @@ __device__ __forceinline__ void red_shared(double *p, double v) {
 
 // Addition into one of the job's FP64 accumulators (ER, EI, EBR, EBI, DEBR, DEBI, back to
 // back from ER).  When the launch stages the whole set in each CTA's shared memory
-// (J.dense > 0: one job on a small mesh) the addition stays in the CTA and the kernel adds
-// the CTA's copy to global memory once at its end; otherwise it is a global reduction.  On
-// a mesh of a few hundred elements the global reductions all land in a handful of L2 lines,
-// whose slice's atomic unit then limits the whole launch.
+// (J.dense > 0: one job on a small mesh, FP32 walks, whose descriptor is a kernel
+// parameter: kStage) the addition stays in the CTA and the kernel adds the CTA's copy to
+// global memory once at its end; otherwise it is a global reduction.  On a mesh of a few
+// hundred elements the global reductions all land in a handful of L2 lines, whose slice's
+// atomic unit then limits the whole launch.
+template <bool kStage>
 __device__ __forceinline__ void acc_add(const JobDev &J, double *p, double v) {
-  if (J.dense) red_shared(reinterpret_cast<double *>(vmc_smem) + (p - J.ER), v);
-  else red_global(p, v);
+  if constexpr (kStage) {
+    if (J.dense) {
+      red_shared(reinterpret_cast<double *>(vmc_smem) + (p - J.ER), v);
+      return;
+    }
+  }
+  red_global(p, v);
 }
 
 __device__ __forceinline__ void add_d(const JobDev &J, double *p, double v) {
-  if (v != 0.0) acc_add(J, p, v);
+  if (v != 0.0) acc_add<false>(J, p, v);
 }
 
 // float -> double by bit manipulation on the integer pipe (exact for normal floats; zero
@@ -212,12 +219,14 @@ __device__ __forceinline__ float d2f_int(double x) {
   return __uint_as_float(r);
 }
 
+template <bool kStage>
 __device__ __forceinline__ void add_f(const JobDev &J, double *p, float v) {
-  if (v != 0.0f) acc_add(J, p, f2d_int(v));
+  if (v != 0.0f) acc_add<kStage>(J, p, f2d_int(v));
 }
 
 // element deposit through the CTA's shared-memory stage when it holds (or can claim) the
 // element's slot, else straight to the global accumulator
+template <bool kStage>
 __device__ __forceinline__ void add_staged(const Stage &S, const JobDev &J, int el, float v) {
   if (v == 0.0f) return;
   const double d = f2d_int(v);
@@ -230,7 +239,7 @@ __device__ __forceinline__ void add_staged(const Stage &S, const JobDev &J, int 
       return;
     }
   }
-  acc_add(J, J.ER + el, d);
+  acc_add<kStage>(J, J.ER + el, d);
 }
 
 // ---- FP32 launch for the tracking form: same draws and sampling laws as CreatePhoton,
