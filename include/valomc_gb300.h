@@ -231,7 +231,9 @@ typedef struct vmc_server_config {
   int32_t max_slots;          /* requests simulated concurrently */
   int32_t use_graph;          /* run each epoch's launches as an updated CUDA graph */
   int64_t memory_budget;      /* bytes of per-request device state admitted at once */
-  int64_t epoch_photons;      /* photons per launch across all slots (latency/throughput knob) */
+  int64_t epoch_photons;      /* photons per launch across all slots; 0 = by load: 50 ms of
+                                 work at the measured rate while the backlog is small, up to
+                                 the backlog and 0.5 s of work as it grows */
   int32_t block_size, blocks_per_sm;
 } vmc_server_config;
 int vmc_server_create(const vmc_server_config *cfg, vmc_server **out);

@@ -49,6 +49,7 @@ struct Request {
   int state = kQueued;
   int status = VMC_OK;
   int inflight = 0;  // launches holding a slice of this request
+  int64_t slice = 0; // photons of this request in the epoch being built
   bool retiring = false;
   Clock::time_point t_submit, t_admit, t_finish;
   double kernel_s = 0;
@@ -110,6 +111,7 @@ void vmc_server::loop() {
   for (;;) {
     std::vector<Request *> admitted;
     std::vector<Request *> batch;
+    int64_t backlog = 0;  // photons not yet issued, active and queued
     {
       std::unique_lock<std::mutex> lk(mu);
       auto has_work = [&] {
@@ -144,6 +146,9 @@ void vmc_server::loop() {
         admitted.push_back(r);
       }
       batch = active;
+      for (Request *r : active)
+        if (r->status == VMC_OK) backlog += r->nphoton - r->issued;
+      for (Request *r : queue) backlog += r->nphoton;
     }
     Lane &L = lanes[cur];
     // L's previous epoch has finished (it was the other lane one iteration ago), so its
@@ -157,13 +162,40 @@ void vmc_server::loop() {
       r->status = upload_job(r->job, *m, cfg.precision, *r->buf, L.st);
     }
     if (!admitted.empty()) cudaStreamSynchronize(L.st);
-    // epoch: a slice of every active request with photons left, one launch per class
-    int64_t epoch = cfg.epoch_photons > 0 ? cfg.epoch_photons
-                                          : std::max<int64_t>(200000, (int64_t)(rate * 0.05));
+    // epoch: a slice of every active request with photons left, one launch per class.  Its
+    // size follows the load: 50 ms of work while the backlog is small (latency), up to the
+    // backlog and at most 0.5 s of work as it grows.  Every launch ends in a drain (CTAs
+    // keep their SM slot until their slowest walk ends); larger epochs pay it less often,
+    // so the loop's capacity rises with the load that needs it.
+    int64_t epoch = cfg.epoch_photons;
+    if (epoch <= 0) {
+      const int64_t lo = std::max<int64_t>(200000, (int64_t)(rate * 0.05));
+      const int64_t hi = std::max<int64_t>(lo, (int64_t)(rate * 0.5));
+      epoch = std::min(hi, std::max(lo, backlog));
+    }
     std::vector<Request *> open;
     for (Request *r : batch)
       if (r->status == VMC_OK && r->issued < r->nphoton) open.push_back(r);
-    const int64_t share = std::max<int64_t>(1, epoch / (int64_t)std::max<size_t>(1, open.size()));
+    // Slices by water-filling: a request with fewer photons left than an equal share of
+    // what remains gets all of them, and the others split the rest equally, so the epoch is
+    // as full as the open requests allow (equal shares left the small requests' unused
+    // share idle: underfilled epochs, a lower measured rate and smaller epochs after them).
+    {
+      std::vector<Request *> by_left(open);
+      std::sort(by_left.begin(), by_left.end(),
+                [](const Request *a, const Request *b) { return a->nphoton - a->issued < b->nphoton - b->issued; });
+      int64_t left = epoch;
+      size_t k = 0;
+      for (; k < by_left.size(); k++) {
+        Request *r = by_left[k];
+        const int64_t s = left / (int64_t)(by_left.size() - k);
+        if (r->nphoton - r->issued > s) break;
+        r->slice = r->nphoton - r->issued;
+        left -= r->slice;
+      }
+      const int64_t s = k < by_left.size() ? std::max<int64_t>(1, left / (int64_t)(by_left.size() - k)) : 0;
+      for (; k < by_left.size(); k++) by_left[k]->slice = std::min(s, by_left[k]->nphoton - by_left[k]->issued);
+    }
     struct Cls { int dim; bool fd; std::vector<Request *> rs; };
     std::vector<Cls> classes;
     for (Request *r : open) {
@@ -186,7 +218,7 @@ void vmc_server::loop() {
       for (Request *r : c.rs) {
         DeviceMesh *m = mesh_impl(meshes[(size_t)r->mesh_id]);
         JobDev d = describe_job(r->job, *m, cfg.precision, *r->buf);
-        int64_t qn = std::min(share, r->nphoton - r->issued);
+        int64_t qn = r->slice;
         d.pcount = qn;
         d.poffset = r->issued;
         descs.push_back(d);
