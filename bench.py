@@ -264,7 +264,9 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=50.0)
     ap.add_argument("--serve-window", type=float, default=10.0)
     ap.add_argument("--serve-epoch", type=float, default=0.0,
-                    help="photons per serving epoch (0: the loop's own choice, ~50 ms of work)")
+                    help="photons per serving epoch (0: the loop's own choice, 50 ms to 0.5 s of work by backlog)")
+    ap.add_argument("--serve-slots", type=int, default=64, help="requests the serving loop simulates at once")
+    ap.add_argument("--serve-block", type=int, default=0, help="threads per CTA of the serving launches (0: default)")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -462,7 +464,8 @@ def bench_serve(args):
     from valomc_gb300 import meshgen as mg
     mix = mg.ServingMix(seed=5)
     meshes = [V.Mesh(b) for b in mix.base]
-    srv = V.Server(max_slots=64, memory_budget=16 << 30, epoch_photons=int(args.serve_epoch))
+    srv = V.Server(max_slots=args.serve_slots, memory_budget=16 << 30, epoch_photons=int(args.serve_epoch),
+                   block_size=args.serve_block)
     ids = [srv.add_mesh(m) for m in meshes]
     # warm the kernels and graphs
     k, p = mix.request()
@@ -492,7 +495,8 @@ def bench_serve(args):
     quarter = max(1, len(lat) // 4)
     q_first, q_last = float(np.median(lat[:quarter])), float(np.median(lat[-quarter:]))
     out = {"metric": "serve p50/p99 latency and photons/s", "unit": "s", "rate_hz": args.serve_rate,
-           "window_s": args.serve_window, "epoch_photons": int(args.serve_epoch), "requests": len(sub),
+           "window_s": args.serve_window, "epoch_photons": int(args.serve_epoch), "slots": args.serve_slots,
+           "block_size": args.serve_block, "requests": len(sub),
            "submit_s": t_sub, "drain_s": wall - t_sub,
            "offered_photons_per_s": offered, "served_photons_per_s": ph / wall,
            "served_steps_per_s": steps / wall, "steps_per_photon": steps / max(ph, 1),
