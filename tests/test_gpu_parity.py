@@ -80,13 +80,16 @@ def test_fp64_matches_oracle_on_same_philox_streams(built, name):
     degenerate = name.startswith("mixed3d")
     tol = 5e-3 if degenerate else PHILOX_L1_TOL
     assert abs(gpu.stats["loss"] - ref.loss) <= (0.002 * n if degenerate else 0)
+    worst = 0.0
     for k in ("ER", "EI", "EBR", "EBI", "DEBR", "DEBI"):
         a, b = getattr(gpu, k), getattr(ref, k)
         den = np.abs(b).sum()
         if den == 0:
             assert np.abs(a).sum() == 0, k
             continue
+        worst = max(worst, np.abs(a - b).sum() / den)
         assert np.abs(a - b).sum() / den < tol, (name, k, np.abs(a - b).sum() / den)
+    print(f"same-streams {name}: worst L1 relative difference {worst:.2e}, steps {gpu.stats['steps']} / {ref.steps}")
     if degenerate:
         assert abs(gpu.stats["steps"] - ref.steps) <= 1e-3 * ref.steps
     else:
@@ -132,6 +135,8 @@ def test_fluence_within_batch_means_error_of_oracle(built, name, precision):
         return np.concatenate([r.ER, r.EI, r.EBR, r.EBI])
 
     frac, chi2, nhit = compare_3sigma(batch_means(gpu, B), batch_means(ref, B))
+    print(f"batch-means {name} {'fp64' if precision == V.VMC_FP64 else 'fp32'}: "
+          f"within 3 sigma {frac:.4f}, chi2/dof {chi2:.3f}, elements {nhit}")
     assert nhit > 50
     # |z| < 3 for a t-like statistic with ~38 dof: expected fraction ~0.995
     assert frac >= 0.985, (name, precision, frac, chi2, nhit)
@@ -144,6 +149,8 @@ def test_energy_balance(built, precision):
     r = V.run(p, precision=precision, nphoton=100000, seed=4, normalize=False)
     L = r.stats["ledger"]
     launched = L["launched"] + L["roulette_gain"] - L["roulette_kill"] - L["lost"]
+    print(f"energy phantom3d {'fp64' if precision == V.VMC_FP64 else 'fp32'}: "
+          f"relative residual {abs(L['absorbed'] + L['exited'] - launched) / L['launched']:.2e}")
     assert r.stats["loss"] == 0
     assert abs(L["absorbed"] + L["exited"] - launched) / L["launched"] < 1e-6, L
 
@@ -156,6 +163,8 @@ def test_energy_balance_against_launched_at_full_phantom(built):
     L = r.stats["ledger"]
     assert r.stats["loss"] == 0 and r.stats["capped"] == 0
     closed = L["launched"] + L["roulette_gain"] - L["roulette_kill"]
+    print(f"energy full phantom fp32: closed residual {abs(L['absorbed'] + L['exited'] - closed) / L['launched']:.2e}, "
+          f"raw {abs(L['absorbed'] + L['exited'] - L['launched']) / L['launched']:.2e}")
     assert abs(L["absorbed"] + L["exited"] - closed) / L["launched"] < 1e-6
     assert abs(L["absorbed"] + L["exited"] - L["launched"]) / L["launched"] < 1e-5
 
@@ -179,6 +188,8 @@ def test_fluence_within_batch_means_error_of_oracle_at_full_phantom(built, preci
         return np.concatenate([r.ER, r.EBR])
 
     frac, chi2, nhit = compare_3sigma(batch_means(gpu, B), batch_means(ref, B))
+    print(f"batch-means full phantom {'fp64' if precision == V.VMC_FP64 else 'fp32'}: "
+          f"within 3 sigma {frac:.4f}, chi2/dof {chi2:.3f}, elements {nhit}")
     assert nhit > 1000
     assert frac >= 0.985, (precision, frac, chi2, nhit)
     assert 0.75 < chi2 < 1.35, (precision, frac, chi2, nhit)
