@@ -149,6 +149,24 @@ def test_server_result_alone_equals_result_in_the_mix(built, precision):
         assert a.stats["steps"] == m.stats["steps"] == one.stats["steps"]
 
 
+def test_server_default_epochs_keep_each_result(built):
+    """Epochs sized by the backlog and water-filled slices (the server's defaults): requests
+    of very different sizes submitted together each equal their run alone."""
+    jobs = small_jobs()
+    sizes = [400, 60000, 3000, 25000]
+    meshes = [V.Mesh(p) for p in jobs]
+    srv = V.Server(max_slots=8, memory_budget=1 << 30)
+    ids = [srv.add_mesh(m) for m in meshes]
+    rids = [srv.submit(ids[k], p, nphoton=n) for k, (p, n) in enumerate(zip(jobs, sizes))]
+    res = [srv.wait(r, timeout_s=120) for r in rids]
+    srv.close()
+    for p, n, r in zip(jobs, sizes, res):
+        one = V.run(p, nphoton=n)
+        assert r.stats["photons_done"] == n and r.stats["steps"] == one.stats["steps"]
+        np.testing.assert_allclose(r.ER, one.ER, rtol=RTOL, atol=1e-300)
+        np.testing.assert_allclose(r.EBR, one.EBR, rtol=RTOL, atol=1e-300)
+
+
 def test_server_admission_by_memory_footprint(built):
     p = cases()["phantom3d"][0]
     mesh = V.Mesh(p)
