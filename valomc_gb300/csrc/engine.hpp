@@ -29,6 +29,10 @@ struct DeviceMesh {
   void *d_geom[2] = {nullptr, nullptr};  // [precision]
   double *d_bnorm = nullptr;
   int64_t bytes = 0;
+  // a mesh that lives for one call: allocated from `pool` and copied, then freed, in order
+  // on `st` (no device-wide synchronisation); resident meshes keep plain allocations
+  cudaMemPool_t pool = nullptr;
+  cudaStream_t st = nullptr;
   ~DeviceMesh();
   const void *geom(int precision) const { return d_geom[precision]; }
 };

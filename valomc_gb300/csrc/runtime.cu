@@ -105,24 +105,27 @@ static int h2d(T *d, const T *h, size_t count, cudaStream_t st) {
 // ---------------------------------------------------------------------------------------
 
 DeviceMesh::~DeviceMesh() {
-  for (void *p : d_geom)
-    if (p) cudaFree(p);
-  if (d_bnorm) cudaFree(d_bnorm);
+  void *ps[] = {d_geom[0], d_geom[1], d_bnorm};
+  for (void *p : ps)
+    if (p) {
+      if (pool) cudaFreeAsync(p, st);
+      else cudaFree(p);
+    }
 }
 
 int upload_mesh(DeviceMesh &m, int precision_mask) {
   const HostMesh &h = m.host;
   m.dim = h.dim;
-  cudaStream_t st = 0;
+  cudaStream_t st = m.st;
   if ((precision_mask & 1) && !m.d_geom[VMC_FP64]) {
     if (h.dim == 3) {
       Tet64 *d;
-      VMC_TRY(dalloc(&d, h.tet64.size(), m.bytes));
+      VMC_TRY(dalloc(&d, h.tet64.size(), m.bytes, m.pool, st));
       m.d_geom[VMC_FP64] = d;
       VMC_TRY(h2d(d, h.tet64.data(), h.tet64.size(), st));
     } else {
       Tri64 *d;
-      VMC_TRY(dalloc(&d, h.tri64.size(), m.bytes));
+      VMC_TRY(dalloc(&d, h.tri64.size(), m.bytes, m.pool, st));
       m.d_geom[VMC_FP64] = d;
       VMC_TRY(h2d(d, h.tri64.data(), h.tri64.size(), st));
     }
@@ -130,18 +133,18 @@ int upload_mesh(DeviceMesh &m, int precision_mask) {
   if ((precision_mask & 2) && !m.d_geom[VMC_FP32]) {
     if (h.dim == 3) {
       Tet32 *d;
-      VMC_TRY(dalloc(&d, h.tet32.size(), m.bytes));
+      VMC_TRY(dalloc(&d, h.tet32.size(), m.bytes, m.pool, st));
       m.d_geom[VMC_FP32] = d;
       VMC_TRY(h2d(d, h.tet32.data(), h.tet32.size(), st));
     } else {
       Tri32 *d;
-      VMC_TRY(dalloc(&d, h.tri32.size(), m.bytes));
+      VMC_TRY(dalloc(&d, h.tri32.size(), m.bytes, m.pool, st));
       m.d_geom[VMC_FP32] = d;
       VMC_TRY(h2d(d, h.tri32.data(), h.tri32.size(), st));
     }
   }
   if (!m.d_bnorm) {
-    VMC_TRY(dalloc(&m.d_bnorm, h.bnorm.size(), m.bytes));
+    VMC_TRY(dalloc(&m.d_bnorm, h.bnorm.size(), m.bytes, m.pool, st));
     VMC_TRY(h2d(m.d_bnorm, h.bnorm.data(), h.bnorm.size(), st));
   }
   VMC_CK(cudaStreamSynchronize(st));
@@ -285,11 +288,18 @@ struct EventGuard {
     if (e) cudaEventDestroy(e);
   }
 };
+// device scratch of one launch: allocated and freed in order on the launch's stream
 template <class T>
 struct DevGuard {
   T *p = nullptr;
+  cudaStream_t st = nullptr;
+  int alloc(size_t count, cudaStream_t s) {
+    st = s;
+    VMC_CK(cudaMallocAsync(reinterpret_cast<void **>(&p), (count ? count : 1) * sizeof(T), s));
+    return VMC_OK;
+  }
   ~DevGuard() {
-    if (p) cudaFree(p);
+    if (p) cudaFreeAsync(p, st);
   }
 };
 struct PinnedGuard {
@@ -453,10 +463,9 @@ int launch_jobs(int device, const LaunchSpec &spec, const std::vector<JobDev> &j
   DevGuard<JobDev> djobs;
   DevGuard<int64_t> dbegin;
   DevGuard<Ctl> dctl;
-  int64_t bytes = 0;
-  VMC_TRY(dalloc(&djobs.p, jobs.size(), bytes));
-  VMC_TRY(dalloc(&dbegin.p, begin.size(), bytes));
-  VMC_TRY(dalloc(&dctl.p, 1, bytes));
+  VMC_TRY(djobs.alloc(jobs.size(), st));
+  VMC_TRY(dbegin.alloc(begin.size(), st));
+  VMC_TRY(dctl.alloc(1, st));
   VMC_TRY(h2d(djobs.p, jobs.data(), jobs.size(), st));
   VMC_TRY(h2d(dbegin.p, begin.data(), begin.size(), st));
   VMC_CK(cudaMemsetAsync(dctl.p, 0, sizeof(Ctl), st));
@@ -740,6 +749,9 @@ int vmc_run(const vmc_input *in, const vmc_options *opt_in, vmc_output *out, vmc
   vmc_stats local;
   vmc_stats *st = stats ? stats : &local;
   memset(st, 0, sizeof(*st));
+  // one stream per call, so calls from several host threads overlap on the device; the
+  // call's device memory is allocated and freed in order on it (it outlives both holders)
+  StreamGuard call_stream;
   DeviceMesh dm;
   dm.device = o.device;
   const int mask = o.precision == VMC_FP64 ? 1 : 2;
@@ -753,13 +765,17 @@ int vmc_run(const vmc_input *in, const vmc_options *opt_in, vmc_output *out, vmc
   // every host-side check of ErrorChecks / Init has passed: now the device
   s = select_device(o.device);
   if (s) return s;
-  s = upload_mesh(dm, mask);
-  if (s) return s;
-  // one stream per call: calls from several host threads overlap on the device
-  StreamGuard call_stream;
   VMC_CK(cudaStreamCreateWithFlags(&call_stream.s, cudaStreamNonBlocking));
   cudaStream_t stream = call_stream.s;
+  cudaMemPool_t call_pool = nullptr;
+  VMC_CK(cudaDeviceGetDefaultMemPool(&call_pool, o.device));
+  dm.pool = call_pool;
+  dm.st = stream;
+  s = upload_mesh(dm, mask);
+  if (s) return s;
   JobBuffers jb;
+  jb.pool = call_pool;
+  jb.free_stream = stream;
   s = upload_job(hj, dm, o.precision, jb, stream);
   if (s) return s;
   JobDev d = describe_job(hj, dm, o.precision, jb);
@@ -768,17 +784,17 @@ int vmc_run(const vmc_input *in, const vmc_options *opt_in, vmc_output *out, vmc
   d.stream = o.stream_id;
   if (o.rng == VMC_RNG_TAPE) {
     const int64_t nw = o.tape_off[in->Nphoton];
-    VMC_TRY(dalloc(&jb.d_tape, (size_t)nw, jb.bytes));
+    VMC_TRY(dalloc(&jb.d_tape, (size_t)nw, jb.bytes, jb.pool, stream));
     VMC_TRY(h2d(jb.d_tape, o.tape, (size_t)nw, stream));
-    VMC_TRY(dalloc(&jb.d_tape_off, (size_t)in->Nphoton + 1, jb.bytes));
+    VMC_TRY(dalloc(&jb.d_tape_off, (size_t)in->Nphoton + 1, jb.bytes, jb.pool, stream));
     VMC_TRY(h2d(jb.d_tape_off, o.tape_off, (size_t)in->Nphoton + 1, stream));
     d.tape = jb.d_tape;
     d.tape_off = jb.d_tape_off;
   }
   const int64_t ntr = std::min<int64_t>(o.trace_photons, in->Nphoton);
   if (ntr > 0) {
-    VMC_TRY(dalloc(&jb.d_trace, (size_t)(ntr * o.trace_stride), jb.bytes));
-    VMC_TRY(dalloc(&jb.d_trace_len, (size_t)ntr, jb.bytes));
+    VMC_TRY(dalloc(&jb.d_trace, (size_t)(ntr * o.trace_stride), jb.bytes, jb.pool, stream));
+    VMC_TRY(dalloc(&jb.d_trace_len, (size_t)ntr, jb.bytes, jb.pool, stream));
     VMC_CK(cudaMemsetAsync(jb.d_trace_len, 0, sizeof(int64_t) * (size_t)ntr, stream));
     d.trace = jb.d_trace;
     d.trace_len = jb.d_trace_len;
@@ -881,6 +897,9 @@ int vmc_run_batch(vmc_mesh *const *meshes, const vmc_input *jobs, int32_t njobs,
   if (o.rng != VMC_RNG_PHILOX) return VMC_ERR_INVALID_ARGUMENT;
   if (!meshes || !jobs || njobs <= 0 || !outs) return VMC_ERR_INVALID_ARGUMENT;
   const int mask = o.precision == VMC_FP64 ? 1 : 2;
+  // one stream per call; the jobs' buffers are allocated and freed in order on it, so it
+  // is declared before them and outlives them
+  StreamGuard call_stream;
   std::vector<HostJob> hj((size_t)njobs);
   std::vector<std::unique_ptr<JobBuffers>> jb((size_t)njobs);
   for (int i = 0; i < njobs; i++) {
@@ -899,9 +918,10 @@ int vmc_run_batch(vmc_mesh *const *meshes, const vmc_input *jobs, int32_t njobs,
   }
   s = select_device(o.device);
   if (s) return s;
-  StreamGuard call_stream;  // one stream per call
   VMC_CK(cudaStreamCreateWithFlags(&call_stream.s, cudaStreamNonBlocking));
   cudaStream_t stream = call_stream.s;
+  cudaMemPool_t call_pool = nullptr;
+  VMC_CK(cudaDeviceGetDefaultMemPool(&call_pool, o.device));
   // group by launch class
   struct Group { LaunchSpec spec; std::vector<int> idx; };
   std::vector<Group> groups;
@@ -929,6 +949,8 @@ int vmc_run_batch(vmc_mesh *const *meshes, const vmc_input *jobs, int32_t njobs,
     std::vector<JobDev> descs;
     for (int i : g.idx) {
       jb[(size_t)i].reset(new JobBuffers);
+      jb[(size_t)i]->pool = call_pool;
+      jb[(size_t)i]->free_stream = stream;
       s = upload_job(hj[(size_t)i], meshes[i]->m, o.precision, *jb[(size_t)i], stream);
       if (s) return s;
       JobDev d = describe_job(hj[(size_t)i], meshes[i]->m, o.precision, *jb[(size_t)i]);
