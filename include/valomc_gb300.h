@@ -131,7 +131,8 @@ typedef struct vmc_options {
   int32_t block_size;       /* threads per block; 0 = tuned default */
   int32_t blocks_per_sm;    /* 0 = as many as fit */
   int32_t fetch_chunk;      /* photons a warp reserves per counter update; 0 = default */
-  int64_t max_steps;        /* per-photon element-step cap (capped photons are reported); 0 = 2^31 */
+  int64_t max_steps;        /* per-photon element-step cap (capped photons are reported); 0 = 10^7,
+                               at most 2^31 - 1 */
   double timeout_s;         /* 0 = none */
   uint32_t stream_id;       /* Philox counter word 3: independent streams for the same seed */
   int32_t normalize;        /* 1 (default when options == NULL): apply MonteCarlo's normalisation */
