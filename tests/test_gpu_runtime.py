@@ -68,6 +68,29 @@ def test_calls_from_two_threads_overlap_and_equal_sequential_runs(built, use_gra
             assert r.stats["steps"] == seq[i].stats["steps"]
 
 
+@pytest.mark.parametrize("precision", [V.VMC_FP64, V.VMC_FP32])
+def test_zero_photon_jobs(built, precision):
+    """An empty run launches nothing and normalises to NaN as the reference does; an empty
+    job inside a batch leaves the others as they are alone."""
+    p = cases()["square2d"][0]
+    r = V.run(p, precision=precision, nphoton=0)
+    assert r.stats["photons_done"] == 0 and r.stats["steps"] == 0
+    assert np.isnan(r.ER).all() and np.isnan(r.EBR).all()
+    raw = V.run(p, precision=precision, nphoton=0, normalize=False)
+    assert not raw.ER.any() and not raw.EBR.any()
+    # a negative count runs no photon and divides by itself, as MonteCarlo does: -0.0
+    neg = V.run(p, precision=precision, nphoton=-5)
+    assert neg.stats["photons_done"] == 0 and not neg.ER.any() and np.signbit(neg.ER).all()
+    jobs = small_jobs()[:2]
+    jobs = [jobs[0].copy(Nphoton=0), jobs[1]]
+    meshes = [V.Mesh(q, precision=precision) for q in jobs]
+    res, tot = V.run_batch(meshes, jobs, precision=precision)
+    assert tot["photons_done"] == jobs[1].Nphoton
+    assert np.isnan(res[0].ER).all()
+    one = V.run(jobs[1], precision=precision)
+    np.testing.assert_allclose(res[1].ER, one.ER, rtol=RTOL, atol=1e-300)
+
+
 def test_batch_through_a_cuda_graph_equals_the_plain_launch(built):
     jobs = small_jobs()
     meshes = [V.Mesh(p) for p in jobs]

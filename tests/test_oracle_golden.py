@@ -58,3 +58,32 @@ def test_reference_binaries_match_fixtures_when_present(built):
     out = oracle.ref_run(p, nthreads=nthr)
     g = np.load(os.path.join(GOLD, "run_square2d.npz"))
     np.testing.assert_array_equal(out["ER"], g["ER"])
+
+
+@pytest.mark.parametrize("name", ["square2d", "phantom3d"])
+def test_zero_photons_normalise_to_nan_as_the_reference(built, name):
+    """An empty run: MonteCarlo divides the zero sums by N = 0 (MC3D.hpp:1792-1818), so every
+    normalised output is NaN; unnormalised they are zero.  Checked against the reference
+    binaries where they are built."""
+    p = CASES[name][0].copy(Nphoton=0)
+    o = oracle.run(p, rng=oracle.RNG_MT, nthreads=1)
+    assert o.status == 0 and np.isnan(o.ER).all() and np.isnan(o.EBR).all()
+    raw = oracle.run(p, rng=oracle.RNG_MT, nthreads=1, normalize=False)
+    assert not raw.ER.any() and not raw.EBR.any()
+    if oracle.have_reference_binaries():
+        ref = oracle.ref_run(p, nthreads=1)
+        for k in ("ER", "EI", "EBR", "EBI", "DEBR", "DEBI"):
+            np.testing.assert_array_equal(np.isnan(getattr(o, k)), np.isnan(ref[k]), err_msg=k)
+
+
+def test_negative_photon_count_runs_none_as_the_reference(built):
+    """MonteCarlo's loop runs no photon for N < 0 and the normalisation divides by N:
+    -0.0 everywhere; bit for bit (signs included) against the reference where built."""
+    p = CASES["square2d"][0].copy(Nphoton=-5)
+    o = oracle.run(p, rng=oracle.RNG_MT, nthreads=1)
+    assert o.status == 0 and not o.ER.any() and np.signbit(o.ER).all()
+    if oracle.have_reference_binaries():
+        ref = oracle.ref_run(p, nthreads=1)
+        for k in ("ER", "EI", "EBR", "EBI", "DEBR", "DEBI"):
+            np.testing.assert_array_equal(getattr(o, k), ref[k], err_msg=k)
+            np.testing.assert_array_equal(np.signbit(getattr(o, k)), np.signbit(ref[k]), err_msg=k)

@@ -761,7 +761,10 @@ int vmc_run(const vmc_input *in, const vmc_options *opt_in, vmc_output *out, vmc
   s = build_job(in, dm.host, hj);
   if (s) return s;
   hj.seed = in->seed_given ? in->seed : clock_seed();
-  if (o.rng == VMC_RNG_TAPE && o.tape_photons < in->Nphoton) return VMC_ERR_INVALID_ARGUMENT;
+  // photons simulated: a negative count runs none, as MonteCarlo's loop does, and is still
+  // the divisor of the normalisation (the reference's -0.0 results)
+  const int64_t nph = std::max<int64_t>(0, in->Nphoton);
+  if (o.rng == VMC_RNG_TAPE && o.tape_photons < nph) return VMC_ERR_INVALID_ARGUMENT;
   // every host-side check of ErrorChecks / Init has passed: now the device
   s = select_device(o.device);
   if (s) return s;
@@ -779,19 +782,19 @@ int vmc_run(const vmc_input *in, const vmc_options *opt_in, vmc_output *out, vmc
   s = upload_job(hj, dm, o.precision, jb, stream);
   if (s) return s;
   JobDev d = describe_job(hj, dm, o.precision, jb);
-  d.pcount = in->Nphoton;
+  d.pcount = nph;
   d.poffset = o.photon_offset;
   d.stream = o.stream_id;
   if (o.rng == VMC_RNG_TAPE) {
-    const int64_t nw = o.tape_off[in->Nphoton];
+    const int64_t nw = o.tape_off[nph];
     VMC_TRY(dalloc(&jb.d_tape, (size_t)nw, jb.bytes, jb.pool, stream));
     VMC_TRY(h2d(jb.d_tape, o.tape, (size_t)nw, stream));
-    VMC_TRY(dalloc(&jb.d_tape_off, (size_t)in->Nphoton + 1, jb.bytes, jb.pool, stream));
-    VMC_TRY(h2d(jb.d_tape_off, o.tape_off, (size_t)in->Nphoton + 1, stream));
+    VMC_TRY(dalloc(&jb.d_tape_off, (size_t)nph + 1, jb.bytes, jb.pool, stream));
+    VMC_TRY(h2d(jb.d_tape_off, o.tape_off, (size_t)nph + 1, stream));
     d.tape = jb.d_tape;
     d.tape_off = jb.d_tape_off;
   }
-  const int64_t ntr = std::min<int64_t>(o.trace_photons, in->Nphoton);
+  const int64_t ntr = std::min<int64_t>(o.trace_photons, nph);
   if (ntr > 0) {
     VMC_TRY(dalloc(&jb.d_trace, (size_t)(ntr * o.trace_stride), jb.bytes, jb.pool, stream));
     VMC_TRY(dalloc(&jb.d_trace_len, (size_t)ntr, jb.bytes, jb.pool, stream));
@@ -954,7 +957,7 @@ int vmc_run_batch(vmc_mesh *const *meshes, const vmc_input *jobs, int32_t njobs,
       s = upload_job(hj[(size_t)i], meshes[i]->m, o.precision, *jb[(size_t)i], stream);
       if (s) return s;
       JobDev d = describe_job(hj[(size_t)i], meshes[i]->m, o.precision, *jb[(size_t)i]);
-      d.pcount = jobs[i].Nphoton;
+      d.pcount = std::max<int64_t>(0, jobs[i].Nphoton);  // a negative count runs none
       d.poffset = o.photon_offset;
       d.stream = o.stream_id;
       descs.push_back(d);
@@ -972,7 +975,7 @@ int vmc_run_batch(vmc_mesh *const *meshes, const vmc_input *jobs, int32_t njobs,
       vmc_stats js;
       memset(&js, 0, sizeof(js));
       js.photons_requested = jobs[i].Nphoton;
-      js.photons_done = jobs[i].Nphoton;
+      js.photons_done = std::max<int64_t>(0, jobs[i].Nphoton);
       js.seed_used = hj[(size_t)i].seed;
       s = collect_job(hj[(size_t)i], meshes[i]->m, *jb[(size_t)i], jobs[i].Nphoton, o.normalize != 0 || !opt_in,
                       &outs[i], &js, stream);

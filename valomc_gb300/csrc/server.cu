@@ -147,8 +147,8 @@ void vmc_server::loop() {
       }
       batch = active;
       for (Request *r : active)
-        if (r->status == VMC_OK) backlog += r->nphoton - r->issued;
-      for (Request *r : queue) backlog += r->nphoton;
+        if (r->status == VMC_OK) backlog += std::max<int64_t>(0, r->nphoton - r->issued);
+      for (Request *r : queue) backlog += std::max<int64_t>(0, r->nphoton);
     }
     Lane &L = lanes[cur];
     // L's previous epoch has finished (it was the other lane one iteration ago), so its
