@@ -115,6 +115,18 @@ def compare_3sigma(a, b):
     return frac, chi2, hit.sum()
 
 
+def chi2_well_sampled(a, b, rel=0.05):
+    """chi2/dof and mean signed z over the elements whose batch means have a relative
+    standard error below `rel` on both sides (near-Gaussian batch means), and their count."""
+    (mg_, sg, hg), (mo, so, ho) = a, b
+    ok = hg & ho
+    ok[ok] = (sg[ok] < rel * np.abs(mg_[ok])) & (so[ok] < rel * np.abs(mo[ok]))
+    if not ok.any():
+        return float("nan"), float("nan"), 0
+    z = (mg_[ok] - mo[ok]) / np.sqrt(sg[ok] ** 2 + so[ok] ** 2)
+    return float(np.mean(z ** 2)), float(np.mean(z)), int(ok.sum())
+
+
 @pytest.mark.parametrize("precision", [V.VMC_FP64, V.VMC_FP32])
 @pytest.mark.parametrize("name", ["square2d", "phantom3d", "phantom3d_fd", "mixed3d", "mixed2d_fd", "circles2d",
                                   "jitter3d"])
@@ -187,9 +199,12 @@ def test_fluence_within_batch_means_error_of_oracle_at_full_phantom(built, preci
         r = oracle.run(p, rng=oracle.RNG_MT, nthreads=os.cpu_count() or 1, nphoton=n_ref, seed=70000 + 1000 * b)
         return np.concatenate([r.ER, r.EBR])
 
-    frac, chi2, nhit = compare_3sigma(batch_means(gpu, B), batch_means(ref, B))
+    a, b = batch_means(gpu, B), batch_means(ref, B)
+    frac, chi2, nhit = compare_3sigma(a, b)
+    well = "; ".join("relative standard error < {:.0%}: chi2/dof {:.3f}, mean z {:+.3f}, elements {}".format(
+        r, *chi2_well_sampled(a, b, r)) for r in (0.05, 0.01))
     print(f"batch-means full phantom {'fp64' if precision == V.VMC_FP64 else 'fp32'}: "
-          f"within 3 sigma {frac:.4f}, chi2/dof {chi2:.3f}, elements {nhit}")
+          f"within 3 sigma {frac:.4f}, chi2/dof {chi2:.3f}, elements {nhit}; {well}")
     assert nhit > 1000
     assert frac >= 0.985, (precision, frac, chi2, nhit)
     assert 0.75 < chi2 < 1.35, (precision, frac, chi2, nhit)

@@ -117,3 +117,28 @@ def test_frequency_domain_tends_to_continuous_wave(built):
     np.testing.assert_allclose(fd.ER[hit], cw.ER[hit], rtol=1e-6)
     assert np.abs(fd.EI).max() < 1e-6 * np.abs(fd.ER).max()
     np.testing.assert_allclose(fd.EBR, cw.EBR, rtol=1e-9, atol=1e-300)
+
+
+@pytest.mark.parametrize("g", [0.0, 0.5])
+def test_backscatter_from_the_beam_axis_matches_the_plain_form(built, g):
+    """A pencil beam along +z into a scattering box (isotropic and forward scattering):
+    the first scatter turns a direction that is exactly on the z axis, the case
+    ScatterPhoton handles apart (MC3D.hpp:1316-1320, dz' = cos(theta) sign(dz)). The FP32
+    form must backscatter there like the plain form: the same absorbed and exited
+    fractions within 5 sigma, and the same mean walk length within 1%."""
+    # the entry point lies on no cell diagonal (x - y and x + y not integers), so the beam
+    # runs inside no face plane
+    p = mg.pencil_box(12, 0.02, 5.0, 0.9, 1.4, (6.35, 5.15), 400000, seed=91)
+    p = p.copy(g=np.full(p.Ne, g))
+    out = {}
+    for prec in FORMS:
+        r = V.run(p, precision=prec, normalize=False)
+        L = r.stats["ledger"]
+        assert r.stats["loss"] == 0 and r.stats["photons_done"] == p.Nphoton
+        out[prec] = (L["absorbed"] / p.Nphoton, L["exited"] / p.Nphoton, r.stats["steps"] / p.Nphoton)
+    a64, e64, s64 = out[V.VMC_FP64]
+    a32, e32, s32 = out[V.VMC_FP32]
+    sig = math.sqrt(2 * a64 * (1 - a64) / p.Nphoton)
+    assert abs(a32 - a64) < 5 * sig, (g, a32, a64, sig)
+    assert abs(e32 - e64) < 5 * sig, (g, e32, e64, sig)
+    assert abs(s32 / s64 - 1) < 0.01, (g, s32, s64)

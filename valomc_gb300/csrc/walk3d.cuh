@@ -455,7 +455,7 @@ struct Walk3D32 {
     if (fabsf(dz) > 0.999f) {
       nx = st * cp;
       ny = st * sp;
-      nz = copysignf(ct, dz);
+      nz = dz > 0.0f ? ct : -ct;  // cos(theta) times the sign of dz (not |cos| with that sign)
     } else {
       const float s2z = 1.0f - dz * dz;
       const float isq = rsqrtf(s2z);
