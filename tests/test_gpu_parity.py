@@ -201,10 +201,14 @@ def test_fluence_within_batch_means_error_of_oracle_at_full_phantom(built, preci
 
     a, b = batch_means(gpu, B), batch_means(ref, B)
     frac, chi2, nhit = compare_3sigma(a, b)
-    well = "; ".join("relative standard error < {:.0%}: chi2/dof {:.3f}, mean z {:+.3f}, elements {}".format(
-        r, *chi2_well_sampled(a, b, r)) for r in (0.05, 0.01))
+    ws = {r: chi2_well_sampled(a, b, r) for r in (0.05, 0.01)}
+    well = "; ".join("relative standard error < {:.0%}: chi2/dof {:.3f}, mean z {:+.3f}, elements {}".format(r, *v)
+                     for r, v in ws.items())
     print(f"batch-means full phantom {'fp64' if precision == V.VMC_FP64 else 'fp32'}: "
           f"within 3 sigma {frac:.4f}, chi2/dof {chi2:.3f}, elements {nhit}; {well}")
+    # a systematic offset shows in the mean signed z of the well-sampled elements long before
+    # it moves the fraction within 3 sigma (a 0.5% FP32 bias near the source read +0.21 / +0.80)
+    assert abs(ws[0.05][1]) < 0.1 and abs(ws[0.01][1]) < 0.3, (precision, ws)
     assert nhit > 1000
     assert frac >= 0.985, (precision, frac, chi2, nhit)
     assert 0.75 < chi2 < 1.35, (precision, frac, chi2, nhit)
