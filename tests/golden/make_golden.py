@@ -76,6 +76,9 @@ def cases():
         # uneven meshes: jittered nodes, random cell diagonals, boundaries from createBH
         "circles2d": (mg.circles_2d(nphoton=20000, seed=321), 2),
         "jitter3d": (mg.jittered_box_3d(nphoton=3000, seed=654), 2),
+        # isotropic scattering of a beam along the z axis: every first scatter takes
+        # ScatterPhoton's on-axis branch, half of them backwards
+        "iso3d": (mg.pencil_box(8, 0.05, 6.0, 0.0, 1.4, (3.35, 4.15), 3000, seed=13), 2),
     }
 
 
@@ -86,7 +89,7 @@ def tape_for(case, nphot=24, words=6000, seed=424242):
 
 
 TRACE_CASES = ["phantom3d", "mixed3d", "mixed3d_fd", "pencil3d", "square2d", "mixed2d", "mixed2d_fd", "circles2d",
-               "jitter3d"]
+               "jitter3d", "iso3d"]
 
 
 def main(only=None):

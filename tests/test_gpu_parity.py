@@ -66,7 +66,7 @@ def test_fp32_replay_follows_reference(built, name):
 
 
 @pytest.mark.parametrize("name", ["phantom3d", "phantom3d_fd", "mixed3d", "mixed3d_fd", "pencil3d", "square2d",
-                                  "mixed2d", "mixed2d_fd", "circles2d", "jitter3d"])
+                                  "mixed2d", "mixed2d_fd", "circles2d", "jitter3d", "iso3d"])
 def test_fp64_matches_oracle_on_same_philox_streams(built, name):
     p = CASES[name][0]
     n = 4000 if p.dim == 3 else 20000
@@ -129,7 +129,7 @@ def chi2_well_sampled(a, b, rel=0.05):
 
 @pytest.mark.parametrize("precision", [V.VMC_FP64, V.VMC_FP32])
 @pytest.mark.parametrize("name", ["square2d", "phantom3d", "phantom3d_fd", "mixed3d", "mixed2d_fd", "circles2d",
-                                  "jitter3d"])
+                                  "jitter3d", "iso3d"])
 def test_fluence_within_batch_means_error_of_oracle(built, name, precision):
     p = CASES[name][0]
     B = 20
