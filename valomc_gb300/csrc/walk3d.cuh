@@ -105,9 +105,11 @@ __device__ __forceinline__ float wrap_phase(float p) { return p >= kTwoPiF ? p -
 
 // distance to the next interaction, -log(U) / mus, with U in (0, 1).  The fast logarithm's
 // absolute error (~1e-7) can make -log(U) of a U within 1e-7 of 1 come out at or just
-// below zero; such a draw is an interaction at once, as it nearly is exactly.
+// below zero; such a draw is an interaction at once, as it nearly is exactly.  The floor is
+// 1e-30 rather than 0 so that a vacuum element (mus = 0) still gets an infinite path, as
+// the reference's -log(U) / 0 does, and never 0 / 0.
 __device__ __forceinline__ float free_path_f(float u, float mus) {
-  return __fdividef(fmaxf(-__logf(u), 0.0f), mus);
+  return __fdividef(fmaxf(-__logf(u), 1e-30f), mus);
 }
 
 // =====================================================================================
