@@ -3,8 +3,10 @@
 // One CTA per SM slot stays resident for the whole run (the replacement of the reference's
 // OpenMP team, cpp/3d/MC3D.hpp:1670-1700).  Every lane carries one photon; when photons
 // end, the warp ballots its dead lanes and hands them the next indices from a warp-owned
-// chunk of the global photon counter (one atomic per chunk), so a warp never runs
-// half-empty while photons remain.  A photon index selects its job (batched launches),
+// chunk of the global photon counter (one atomic per chunk), once refill_min lanes are
+// idle or on every 8th iteration, so a warp never runs half-empty for long while photons
+// remain.  A one-job launch on a small mesh stages the job's accumulators in shared memory
+// (LaunchParams::dense) and adds them to the job's arrays when the CTA ends.  A photon index selects its job (batched launches),
 // its Philox stream (key = job seed, counter = photon index) or its tape segment, and the
 // walk advances one element step per loop iteration.  Each loop iteration polls nothing
 // but registers; the host cancel flag is read every 1024 iterations.

@@ -1,6 +1,6 @@
 // server.cu -- serving loop: resident meshes, requests admitted into slots by their
-// device-memory footprint, continuous batching of all admitted requests into short
-// persistent launches ("epochs").
+// device-memory footprint, continuous batching of all admitted requests into persistent
+// launches ("epochs") sized by the backlog (50 ms of work when it is small, up to 0.5 s).
 //
 // Epochs alternate between two streams ("lanes"): the next epoch is queued while the
 // current one runs, so it takes the SMs as the running launch drains.
