@@ -63,3 +63,47 @@ def test_header_is_c99_and_the_library_links(built):
     assert e0.count(1) == 1 and e1.count(0) == 1  # the shared edge, seen from both sides
     boundary = sorted(-1 - x for x in hn if x < 0)
     assert boundary == [0, 1, 2, 3]  # each boundary edge once, as -1 - ib
+
+
+LAYOUT = r"""
+#include <stddef.h>
+#include <stdio.h>
+#include "valomc_gb300.h"
+#define F(T, m) printf(#T " " #m " %zu\n", offsetof(T, m))
+#define S(T) printf(#T " sizeof %zu\n", sizeof(T))
+int main(void) {
+%BODY%
+  return 0;
+}
+"""
+
+
+@pytest.mark.skipif(shutil.which("gcc") is None, reason="no C compiler")
+def test_python_structs_have_the_headers_layout(built):
+    """Every ctypes mirror of a header struct (valomc_gb300/api.py) has the C compiler's size
+    and field offsets, so no field is missing, added or misplaced on either side."""
+    from valomc_gb300 import api
+    pairs = {"vmc_input": api.VmcInput, "vmc_output": api.VmcOutput, "vmc_options": api.VmcOptions,
+             "vmc_stats": api.VmcStats, "vmc_server_config": api.VmcServerConfig,
+             "vmc_noalloc_buffers": api.VmcNoallocBuffers}
+    body = []
+    for cname, py in pairs.items():
+        body.append(f"  S({cname});")
+        body += [f"  F({cname}, {f[0]});" for f in py._fields_]
+    with tempfile.TemporaryDirectory() as td:
+        src, exe = os.path.join(td, "layout.c"), os.path.join(td, "layout")
+        with open(src, "w") as fp:
+            fp.write(LAYOUT.replace("%BODY%", "\n".join(body)))
+        subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), src, "-o", exe],
+                       check=True, capture_output=True, text=True)
+        lines = subprocess.run([exe], check=True, capture_output=True, text=True, timeout=60).stdout.split("\n")
+    c = {}
+    for ln in lines:
+        if ln.strip():
+            t, m, v = ln.split()
+            c[(t, m)] = int(v)
+    import ctypes
+    for cname, py in pairs.items():
+        assert c[(cname, "sizeof")] == ctypes.sizeof(py), cname
+        for f in py._fields_:
+            assert c[(cname, f[0])] == getattr(py, f[0]).offset, (cname, f[0])
