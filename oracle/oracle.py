@@ -88,8 +88,9 @@ def build(quiet=True):
     subprocess.run(cmd, check=True, capture_output=quiet)
 
 
-# the reference tree, where the checker's recipes read it (the Makefile's REF)
-REF_TREE = os.environ.get("REF", "/root/reference")
+# the reference tree the checker's recipes read (the Makefile's REF): by default the copy
+# staged under baseline/_ref/ValoMC, which goes with the working tree to a GPU host
+REF_TREE = os.environ.get("REF", os.path.join(os.path.dirname(HERE), "baseline", "_ref", "ValoMC"))
 
 
 def reference_file(rel):

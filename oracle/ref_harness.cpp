@@ -14,7 +14,7 @@
  * Input files use the reference executable's text format (cpp/3d/MC3D.cpp:97-179,
  * cpp/2d/MC2D.cpp:125-203) and are read with the reference's own reader (cpp/fileio.hpp).
  *
- *   timed:  <bin> input.txt output.txt nthreads
+ *   timed:  <bin> input.txt output.txt nthreads   (output "-": only the statistics line, on stdout)
  *   trace:  <bin> input.txt tape.bin output.txt
  * tape.bin: int64 nphot, int64 off[nphot+1], uint32 words[off[nphot]].
  */
@@ -188,13 +188,17 @@ int main(int argc, char **argv) {
   MC.MonteCarlo(progress_cb, finalchecks_cb);
   auto t1 = std::chrono::steady_clock::now();
   double secs = std::chrono::duration<double>(t1 - t0).count();
-  FILE *fo = fopen(argv[2], "w");
-  if (!fo) return 1;
 #ifdef USE_OMP
   int used = omp_get_max_threads();
 #else
   int used = 1;
 #endif
+  if (strcmp(argv[2], "-") == 0) {  /* timing only: the statistics line on stdout, no arrays */
+    printf("STATS seconds %.9f loss %ld threads %d nphoton %ld\n", secs, (long)MC.loss, used, (long)MC.Nphoton);
+    return 0;
+  }
+  FILE *fo = fopen(argv[2], "w");
+  if (!fo) return 1;
   fprintf(fo, "STATS seconds %.9f loss %ld threads %d nphoton %ld\n", secs, (long)MC.loss, used, (long)MC.Nphoton);
   dump_arrays(fo);
   fclose(fo);
