@@ -18,7 +18,8 @@
  *   - Device memory is owned by the library (per call, or by a resident mesh handle).
  *   - vmc_run and vmc_run_batch each run on a non-blocking stream of their own, so calls
  *     from several host threads overlap on the GPU; a resident mesh may be shared by
- *     concurrent calls (they only read it). vmc_run_noalloc is the exception (below).
+ *     concurrent calls (they only read it).  vmc_run_noalloc also runs on a stream of its
+ *     own, but its calls share one scratch array and must not overlap (below).
  */
 #ifndef VALOMC_GB300_H
 #define VALOMC_GB300_H
@@ -266,6 +267,14 @@ int vmc_server_destroy(vmc_server *s);
 /* - Every call reuses the same scratch and clears what must start at zero; calls that   */
 /*   overlap on the GPU (other threads, other streams) race on it: serialise them.       */
 /* - It calls no cudaMalloc, cudaFree or other allocating device routine.                */
+/* - It runs on a non-blocking stream of its own and returns when its work is done; it   */
+/*   does not wait for the caller's streams, so no work in flight may still use `dev`.   */
+/* - `dev` must be device memory of options.device, the device the mesh lives on; other  */
+/*   pointers are refused (VMC_ERR_INVALID_ARGUMENT).                                    */
+/* - It polls no progress callback, cancel flag or timeout (options that set one are     */
+/*   refused); use_graph and stage_slots are not used.                                   */
+/* - The cached scratch address belongs to the device's primary context: after           */
+/*   cudaDeviceReset on a device, do not call it on that device again.                   */
 #define VMC_NOALLOC_SCRATCH_BYTES (256 * 1024)
 #define VMC_NOALLOC_MAX_SOURCES 512
 

@@ -7,14 +7,20 @@
 // the pool kernel's scratch -- the launch control block, the one-entry job table, the
 // rare-event counter slots and the emitting-face records -- is one file-scope device
 // array of a fixed size, held by every GPU that loads the library until the process
-// exits.  The kernel is the same photon-pool kernel vmc_run launches; only where its
-// scratch lives differs.
+// exits.  The kernel is the per-job form of the photon-pool kernel, the one multi-job
+// batches launch: it reads the job descriptor from the job table in global memory (here in
+// the scratch array).  vmc_run launches a single FP32 job in the one-job form, whose
+// descriptor and Philox round keys are kernel parameters.  Both walk the same photons to
+// the same results; the per-job form runs a few percent slower.
 //
 // In host code `g_scratch` names a host-side stand-in, not a device address, so the
 // address is looked up once per device (with that device current) by
-// cudaGetSymbolAddress and passed to the kernel.  Every call reuses the array: the counters
-// that must start at zero are cleared at each call, and calls that overlap on the GPU race
-// on it.
+// cudaGetSymbolAddress and passed to the kernel.  The cached address belongs to the
+// device's primary context: it does not survive cudaDeviceReset, so a process that resets
+// a device must not call vmc_run_noalloc on it again.  Every call reuses the array: the
+// counters that must start at zero are cleared at each call, and calls that overlap on the
+// GPU race on it.  Each call runs on a non-blocking stream of its own, like the other entry
+// points, and waits for it before returning.
 #include <cuda_runtime.h>
 #include <string.h>
 
@@ -72,6 +78,30 @@ int scratch_address(int device, unsigned char **out) {
   return VMC_OK;
 }
 
+// a caller buffer must be device memory of the launch device (a host pointer, or another
+// GPU's memory, would fault in the kernel)
+int check_device_buffer(const void *p, int device, const char *name) {
+  cudaPointerAttributes a;
+  cudaError_t e = cudaPointerGetAttributes(&a, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_error(std::string("vmc_run_noalloc: ") + name + " is not a device pointer");
+    return VMC_ERR_INVALID_ARGUMENT;
+  }
+  if ((a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged) || a.device != device) {
+    set_error(std::string("vmc_run_noalloc: ") + name + " must be device memory of device " + std::to_string(device));
+    return VMC_ERR_INVALID_ARGUMENT;
+  }
+  return VMC_OK;
+}
+
+struct OwnStream {
+  cudaStream_t s = nullptr;
+  ~OwnStream() {
+    if (s) cudaStreamDestroy(s);
+  }
+};
+
 template <class T>
 int put(unsigned char *base, size_t off, const T *src, size_t count, cudaStream_t st) {
   if (!count) return VMC_OK;
@@ -94,7 +124,16 @@ extern "C" int vmc_run_noalloc(vmc_mesh *mesh, const vmc_input *job, const vmc_o
     set_error("vmc_run_noalloc runs Philox streams only (no tape, no trace)");
     return VMC_ERR_INVALID_ARGUMENT;
   }
+  if (o.progress || o.cancel || o.timeout_s > 0) {
+    set_error("vmc_run_noalloc does not poll a progress callback, a cancel flag or a timeout");
+    return VMC_ERR_INVALID_ARGUMENT;
+  }
   DeviceMesh *m = mesh_impl(mesh);
+  if (m->device != o.device) {
+    set_error("vmc_run_noalloc: the mesh lives on device " + std::to_string(m->device) + ", options.device is " +
+              std::to_string(o.device));
+    return VMC_ERR_INVALID_ARGUMENT;
+  }
   if (!(mesh_precision_mask(mesh) & (o.precision == VMC_FP64 ? 1 : 2))) return VMC_ERR_INVALID_ARGUMENT;
   // host half: ErrorChecks + Init on the mesh's geometry
   vmc_input in = *job;
@@ -115,12 +154,17 @@ extern "C" int vmc_run_noalloc(vmc_mesh *mesh, const vmc_input *job, const vmc_o
   }
   s = select_device(o.device);
   if (s) return s;
+  if ((s = check_device_buffer(dev->optics, o.device, "optics")) || (s = check_device_buffer(dev->bctype, o.device, "bctype")) ||
+      (s = check_device_buffer(dev->bcn, o.device, "bcn")) || (s = check_device_buffer(dev->acc, o.device, "acc")))
+    return s;
   unsigned char *base = nullptr;
   s = scratch_address(o.device, &base);
   if (s) return s;
   const int64_t Ne = m->host.Ne, Nb = m->host.Nb;
   const size_t rows = hj.homogeneous ? 1 : (size_t)Ne;
-  cudaStream_t st = 0;
+  OwnStream own;
+  VMC_CK(cudaStreamCreateWithFlags(&own.s, cudaStreamNonBlocking));
+  cudaStream_t st = own.s;
   // the job's arrays into the caller's buffers
   std::vector<float> optf;
   if (o.precision == VMC_FP64) {
@@ -218,10 +262,11 @@ extern "C" int vmc_run_noalloc(vmc_mesh *mesh, const vmc_input *job, const vmc_o
   std::vector<double> h((size_t)(2 * Ne + 4 * Nb));
   std::vector<unsigned long long> jc((size_t)kSlots * kJcN);
   std::vector<double> lg((size_t)kSlots * kLgN);
-  VMC_CK(cudaMemcpy(&hc, base + kOffCtl, sizeof(Ctl), cudaMemcpyDeviceToHost));
-  VMC_CK(cudaMemcpy(h.data(), acc, h.size() * sizeof(double), cudaMemcpyDeviceToHost));
-  VMC_CK(cudaMemcpy(jc.data(), base + kOffJc, jc.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
-  VMC_CK(cudaMemcpy(lg.data(), base + kOffLedger, lg.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  VMC_CK(cudaMemcpyAsync(&hc, base + kOffCtl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+  VMC_CK(cudaMemcpyAsync(h.data(), acc, h.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+  VMC_CK(cudaMemcpyAsync(jc.data(), base + kOffJc, jc.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+  VMC_CK(cudaMemcpyAsync(lg.data(), base + kOffLedger, lg.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+  VMC_CK(cudaStreamSynchronize(st));
   const double *ER = h.data(), *EI = ER + Ne, *EBR = EI + Ne, *EBI = EBR + Nb, *DEBR = EBI + Nb, *DEBI = DEBR + Nb;
   normalise(m->host, hj, in.Nphoton, ER, EI, EBR, EBI, DEBR, DEBI, out, o.normalize != 0 || !opt_in);
   if (out->HN) memcpy(out->HN, m->host.HN.data(), m->host.HN.size() * sizeof(int64_t));
