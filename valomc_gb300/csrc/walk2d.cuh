@@ -16,7 +16,11 @@ __device__ __forceinline__ bool ray_seg(const double R[2], const double D[2], co
                                         double &t) {
   double det = D[0] * (U[1] - V[1]) - D[1] * (U[0] - V[0]);
   if ((-kDblEps < det) && (det < kDblEps)) return false;
-  double s = (D[1] * (R[0] - U[0]) - D[0] * (R[1] - U[1])) / det;
+  const double ns = D[1] * (R[0] - U[0]) - D[0] * (R[1] - U[1]);
+  // s = ns / det < 0 exactly when ns and det have opposite signs (the quotient of nonzero
+  // coordinate differences cannot round to zero), decided before the division
+  if ((ns < 0.0) != (det < 0.0) && ns != 0.0) return false;
+  double s = ns / det;
   if ((s < 0.0) || (s > 1.0)) return false;
   t = ((R[1] - U[1]) * (U[0] - V[0]) - (R[0] - U[0]) * (U[1] - V[1])) / det;
   return true;
@@ -99,12 +103,20 @@ struct Walk2D64 {
     return false;
   }
 
-  // Normal(el, f), MC2D.hpp:358-387
-  __device__ __forceinline__ static void edge_normal(const double V[3][2], int f, double nor[2]) {
-    const int i0 = f, i1 = f == 2 ? 0 : f + 1;
-    double ddx = V[i1][0] - V[i0][0], ddy = V[i1][1] - V[i0][1];
+  // Normal(el, f), MC2D.hpp:358-387: the unit normal of the edge from a to b
+  __device__ __forceinline__ static void normal_of(const double a[2], const double b[2], double nor[2]) {
+    double ddx = b[0] - a[0], ddy = b[1] - a[1];
     double norm = sqrt(ddx * ddx + ddy * ddy);
     nor[0] = ddy / norm; nor[1] = -ddx / norm;
+  }
+  // Edge f runs from vertex f to vertex f + 1 (mod 3); constant indices in each case keep
+  // the vertex array in registers (an index computed from f would put it in local memory).
+  __device__ __forceinline__ static void edge_normal(const double V[3][2], int f, double nor[2]) {
+    switch (f) {
+      case 0: normal_of(V[0], V[1], nor); break;
+      case 1: normal_of(V[1], V[2], nor); break;
+      default: normal_of(V[2], V[0], nor); break;
+    }
   }
 
   __device__ bool roulette(const JobDev &J, R &rng) {

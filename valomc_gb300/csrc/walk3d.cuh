@@ -28,9 +28,14 @@ __device__ __forceinline__ bool ray_tri(const double O[3], const double D[3], co
   double pv[3] = {D[1] * e2[2] - D[2] * e2[1], D[2] * e2[0] - D[0] * e2[2], D[0] * e2[1] - D[1] * e2[0]};
   double det = e1[0] * pv[0] + e1[1] * pv[1] + e1[2] * pv[2];
   if ((-kDblEps < det) && (det < kDblEps)) return false;
-  double inv = 1.0 / det;
   double tv[3] = {O[0] - V0[0], O[1] - V0[1], O[2] - V0[2]};
-  double u = (tv[0] * pv[0] + tv[1] * pv[1] + tv[2] * pv[2]) * inv;
+  const double du = tv[0] * pv[0] + tv[1] * pv[1] + tv[2] * pv[2];
+  // u = du / det < 0 exactly when du and det have opposite signs (their product cannot
+  // round to zero: |du| is far above 2^-1074 |det| for any nonzero coordinate
+  // differences), so that half of the rejections is decided before the division
+  if ((du < 0.0) != (det < 0.0) && du != 0.0) return false;
+  double inv = 1.0 / det;
+  double u = du * inv;
   if ((u < 0.0) || (u > 1.0)) return false;
   double qv[3] = {tv[1] * e1[2] - tv[2] * e1[1], tv[2] * e1[0] - tv[0] * e1[2], tv[0] * e1[1] - tv[1] * e1[0]};
   double v = (D[0] * qv[0] + D[1] * qv[1] + D[2] * qv[2]) * inv;
@@ -347,16 +352,25 @@ struct Walk3D64 {
     return kAlive;
   }
 
-  // Normal(el, f), MC3D.hpp:408-457
-  __device__ __forceinline__ static void face_normal(const double V[4][3], int f, double nor[3]) {
-    const int i0 = f == 3 ? 1 : 0;
-    const int i1 = f == 0 ? 1 : f == 1 ? 1 : 2;
-    const int i2 = f == 0 ? 2 : 3;
-    double x1 = V[i1][0] - V[i0][0], y1 = V[i1][1] - V[i0][1], z1 = V[i1][2] - V[i0][2];
-    double x2 = V[i2][0] - V[i0][0], y2 = V[i2][1] - V[i0][1], z2 = V[i2][2] - V[i0][2];
+  // Normal(el, f), MC3D.hpp:408-457: the unit normal of the face through vertices a, b, c
+  __device__ __forceinline__ static void normal_of(const double a[3], const double b[3], const double c[3],
+                                                   double nor[3]) {
+    double x1 = b[0] - a[0], y1 = b[1] - a[1], z1 = b[2] - a[2];
+    double x2 = c[0] - a[0], y2 = c[1] - a[1], z2 = c[2] - a[2];
     double nx = y1 * z2 - z1 * y2, ny = z1 * x2 - x1 * z2, nz = x1 * y2 - y1 * x2;
     double norm = sqrt(nx * nx + ny * ny + nz * nz);
     nor[0] = nx / norm; nor[1] = ny / norm; nor[2] = nz / norm;
+  }
+  // Face f of the tetrahedron is (0,1,2), (0,1,3), (0,2,3) or (1,2,3).  Each case names its
+  // vertices with constant indices, so the vertex array stays in registers (an index
+  // computed from f would put it in local memory for the whole step).
+  __device__ __forceinline__ static void face_normal(const double V[4][3], int f, double nor[3]) {
+    switch (f) {
+      case 0: normal_of(V[0], V[1], V[2], nor); break;
+      case 1: normal_of(V[0], V[1], V[3], nor); break;
+      case 2: normal_of(V[0], V[2], V[3], nor); break;
+      default: normal_of(V[1], V[2], V[3], nor); break;
+    }
   }
 };
 
