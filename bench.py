@@ -1,25 +1,32 @@
-"""Benchmark of the photon-propagation path on the 60x60x30 mm inclusion phantom
-(648 000 tetrahedra, 1 mm grid, Gaussian sigma = 1 mm direct source, Fresnel boundary).
+"""Benchmark of the photon-propagation path, every workload of the brief in one line.
 
-A step is one simulation of ``--photons`` photons (default 1e8) through the FP32 tracking
-form with the mesh resident on the device.  Reported:
-  value       photons/s with the mesh and job resident (whole-job: setup of the job,
-              kernel, read-back), max over ranks
-  e2e         photons/s through vmc_run with host buffers: setup, uploads, kernel and the
-              read-back of all results inside the timed region
-  fp64        the plain FP64 form on the same workload (photons/s) and the ratio
-  roofline    the pool kernel's algorithmic gather bytes (108 B per CW element step, the
-              per-step record of the reference layout) over its CUDA-event duration,
-              against the measured HBM copy bandwidth; the measured L2 random-gather
-              ceiling is reported beside it
-  cpu_baseline the CPU oracle (OpenMP restatement of the reference engine) on all host
-              cores on a bounded sample of the same workload
-  matched_error  chi2/dof of FP32-form batch means against FP64-form batch means (1 means
-              the FP32 form has no error beyond the Monte Carlo noise)
-  serve       p50/p99 latency and photons/s of a short Poisson request stream
+Headline (the JSON line's value): the 60x60x30 mm inclusion phantom (648 000 tetrahedra,
+1 mm grid, Gaussian sigma = 1 mm direct source, Fresnel boundary).  A step is one
+simulation of ``--photons`` photons (default 1e8) through the FP32 tracking form with the
+mesh resident on the device.
+
+  value        photons/s with the mesh resident (per step: the job's setup and upload, the
+               kernel and the read-back), max over ranks
+  e2e          photons/s through vmc_run with host buffers: setup, uploads, kernel and the
+               read-back of all results inside the timed region
+  roofline     the pool kernel's algorithmic gather bytes (108 B per CW element step) over
+               its CUDA-event duration, against the measured HBM copy bandwidth; the kernel
+               is bound by instruction issue, with the measured L2 dependent-gather ceiling
+               as its memory ceiling (l2_gather_frac), and runs at the SIMT efficiency of
+               the committed ncu profile
+  cpu_baseline the reference engine itself (MonteCarlo() of cpp/3d/MC3D.hpp, built with
+               the reference's own flags -O3 -DUSE_OMP -fopenmp) on all host cores, on a
+               bounded sample of the same workload; the CPU oracle where it is not built
+  fp64         the plain FP64 form on the same workload
+  matched_error  per-element error of each GPU form against the FP64 CPU oracle, as the
+               ratio to the Monte Carlo noise floor (1 = no error beyond the noise)
+  configs      the other workloads: the 2D square (plain FP64 and FP32, against the
+               reference's 2D engine), the frequency-domain phantom, 64 batched instances in
+               one persistent launch, and the serving loop at 50 requests/s
 The L2 (129 MB) is flushed between timed steps by writing a 512 MB buffer.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+    python bench.py --config fd|batch|serve|square2d     (one workload, one line)
 """
 import argparse
 import json
@@ -27,7 +34,7 @@ import math
 import os
 import subprocess
 import sys
-import threading
+import tempfile
 import time
 
 import numpy as np
@@ -36,8 +43,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 BYTES_PER_STEP_CW = 108  # element nodes 16 + coordinates 48 + HN row 16 + optics 12 + ER RMW 16
+BYTES_PER_STEP_FD = 128  # + k 4 + EI RMW 16
 METRIC = "photons/s FP32-track vs FP64 GPU at matched fluence error; serve p50/p99 latency"
 WORKLOAD = "inclusion phantom 60x60x30 mm, 648000 tets, gaussian sigma 1 mm direct source, CW"
+REF_BIN = os.path.join(ROOT, "oracle", "_ref")
 
 
 def dist_env():
@@ -62,21 +71,19 @@ class Dist:
         if self.ws > 1:
             self.td.barrier()
 
-    def max(self, v):
+    def _reduce(self, v, op):
         if self.ws == 1:
             return v
         import torch
         t = torch.tensor([float(v)], dtype=torch.float64)
-        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        self.td.all_reduce(t, op=op)
         return float(t.item())
 
+    def max(self, v):
+        return self._reduce(v, self.td.ReduceOp.MAX if self.ws > 1 else None)
+
     def sum(self, v):
-        if self.ws == 1:
-            return v
-        import torch
-        t = torch.tensor([float(v)], dtype=torch.float64)
-        self.td.all_reduce(t, op=self.td.ReduceOp.SUM)
-        return float(t.item())
+        return self._reduce(v, self.td.ReduceOp.SUM if self.ws > 1 else None)
 
     def close(self):
         if self.ws > 1:
@@ -152,99 +159,300 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic():
-    """DRAM bytes per element step of the FP32 pool kernel from the committed ncu summary."""
+def ncu_profile():
+    """DRAM bytes per element step, threads per warp instruction and issue activity of the
+    FP32 pool kernel, from the committed ncu summary (profiles/)."""
     path = os.path.join(ROOT, "profiles", "pool_kernel_fp32_phantom.json")
     if os.path.exists(path):
         with open(path) as fp:
-            d = json.load(fp)
-        return d.get("dram_bytes_per_step")
-    return None
+            return json.load(fp)
+    return {}
 
 
-def cpu_baseline(p, seconds_target=12.0, threads=None, name="phantom"):
-    """The CPU oracle on all host cores, on a sample sized to ~seconds_target of work."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle
-    oracle.build()
-    threads = threads or os.cpu_count() or 1
-    probe = max(threads * 400, 2000)
-    r = oracle.run(p, rng=oracle.RNG_MT, nthreads=threads, nphoton=probe, normalize=False)
-    rate = probe / max(r.seconds, 1e-6)
-    n = int(min(max(rate * seconds_target, probe), 5e6))
-    r = oracle.run(p, rng=oracle.RNG_MT, nthreads=threads, nphoton=n, normalize=False)
-    rate = n / r.seconds
-    return {"value": rate, "unit": "photons/s", "cores": threads, "kind": "port",
-            "sample": f"{n} photons of the {name} workload (MT19937, {threads} OpenMP threads), "
-                      f"{r.seconds:.1f} s", "steps_per_photon": r.steps / n}
+# ---------------------------------------------------------------------------------------
+# CPU side: the reference engine itself where it is built, else the oracle
+# ---------------------------------------------------------------------------------------
+
+def reference_binary(dim):
+    path = os.path.join(REF_BIN, "ref3d_time" if dim == 3 else "ref2d_time")
+    return path if os.path.exists(path) else None
+
+
+class CpuBaseline:
+    """Times MonteCarlo() on the host's cores on bounded samples of a workload: the
+    reference's own engine (kind "reference") where oracle/_ref was built from the
+    reference tree, else the oracle (the restatement, kind "port")."""
+
+    def __init__(self, p, name, threads=None):
+        self.p, self.name = p, name
+        self.threads = threads or os.cpu_count() or 1
+        self.exe = reference_binary(p.dim)
+        self.kind = "reference" if self.exe else "port"
+        self.tmp = None
+        self.files = {}
+
+    def _input(self, n):
+        from valomc_gb300 import meshgen
+        if n not in self.files:
+            if self.tmp is None:
+                self.tmp = tempfile.TemporaryDirectory()
+            path = os.path.join(self.tmp.name, f"in_{n}.txt")
+            meshgen.write_input(path, self.p.copy(Nphoton=n, seed=777))
+            self.files[n] = path
+        return self.files[n]
+
+    def run(self, n):
+        """Seconds of MonteCarlo() for n photons and the element steps (None for the engine)."""
+        if self.exe:
+            out = subprocess.run([self.exe, self._input(n), "-", str(self.threads)], capture_output=True, text=True,
+                                 check=True).stdout.split()
+            return float(out[out.index("seconds") + 1]), None
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        oracle.build()
+        r = oracle.run(self.p, rng=oracle.RNG_MT, nthreads=self.threads, nphoton=n, seed=777, normalize=False)
+        return r.seconds, r.steps
+
+    def size_for(self, seconds):
+        probe = max(self.threads * 200, 2000)
+        s, _ = self.run(probe)
+        return int(min(max(probe / max(s, 1e-6) * seconds, probe), 2e7))
+
+    def describe(self, n, s):
+        src = "cpp/3d/MC3D.hpp" if self.p.dim == 3 else "cpp/2d/MC2D.hpp"
+        who = (f"the reference's MonteCarlo() ({src}, -O3 -DUSE_OMP -fopenmp)" if self.kind == "reference"
+               else "the CPU oracle (the reference's algorithm restated, MT19937)")
+        return {"value": n / s, "unit": "photons/s", "cores": self.threads, "kind": self.kind,
+                "sample": f"{n} photons of the {self.name} workload, {who}, {self.threads} OpenMP threads, "
+                          f"{s:.1f} s of MonteCarlo()"}
 
 
 def reference_arm(args):
+    """The reference's CPU implementation of the path on all host cores, each step a
+    bounded sample of the phantom workload (rank 0 only)."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
     from valomc_gb300 import meshgen as mg
     p = mg.config_3d_phantom(nphoton=1, seed=12345)
-    vals = []
-    base = None
-    for i in range(args.warmup + args.steps):
-        b = cpu_baseline(p, seconds_target=args.ref_seconds)
+    cb = CpuBaseline(p, "phantom")
+    steps = args.warmup + args.steps
+    n = cb.size_for(max(2.0, args.ref_budget / steps))
+    secs = []
+    for i in range(steps):
+        s, _ = cb.run(n)
         if i >= args.warmup:
-            vals.append(b["value"])
-            base = b
-    v = float(np.mean(vals))
+            secs.append(s)
+    t = float(np.mean(secs))
+    v = n / t
+    base = cb.describe(n, t)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "photons/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * args.ref_seconds,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * t,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": WORKLOAD},
-            "cpu_baseline": {"value": v, "unit": "photons/s", "cores": base["cores"], "kind": "port",
-                             "sample": base["sample"]},
+            "data": "synthetic", "config": {"workload": WORKLOAD, "photons_per_step": n},
+            "cpu_baseline": base,
             "e2e": {"value": v, "unit": "photons/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
 
 
-def serve_run(seconds, rate_hz, seed=5):
-    """Poisson request stream against resident meshes (smaller budgets than the full mix so
-    the run stays short): returns latency percentiles and aggregate photons/s."""
+# ---------------------------------------------------------------------------------------
+# matched error: each GPU form against the FP64 CPU oracle, per element
+# ---------------------------------------------------------------------------------------
+
+def welch_error_to_noise(gpu_rows, ref_rows, rel=0.05):
+    """Over elements whose batch means have a relative standard error below `rel` on both
+    sides: chi2/dof of the Welch t statistics, its t-expectation mean(nu / (nu - 2)), the
+    fraction within the 3-sigma t quantile, and the error-to-noise ratio
+    sqrt(chi2 / expectation) (1: the GPU form's error is the Monte Carlo noise)."""
+    from scipy.stats import t as student_t
+    g, r = np.asarray(gpu_rows), np.asarray(ref_rows)
+    Bg, Br = len(g), len(r)
+    gm, gv = g.mean(0), g.var(0, ddof=1) / Bg
+    rm, rv = r.mean(0), r.var(0, ddof=1) / Br
+    ok = np.all(g != 0, axis=0) & np.all(r != 0, axis=0)
+    ok[ok] = (np.sqrt(gv[ok]) < rel * np.abs(gm[ok])) & (np.sqrt(rv[ok]) < rel * np.abs(rm[ok]))
+    s2 = gv[ok] + rv[ok]
+    t = (gm[ok] - rm[ok]) / np.sqrt(s2)
+    nu = s2 ** 2 / (gv[ok] ** 2 / (Bg - 1) + rv[ok] ** 2 / (Br - 1))
+    e = float(np.mean(nu / (nu - 2)))
+    chi2 = float(np.mean(t * t))
+    q = student_t.ppf(0.5 + 0.99730020393674 / 2, nu)
+    return {"elements": int(ok.sum()), "chi2_per_dof": chi2, "t_expectation": e,
+            "error_to_noise": math.sqrt(chi2 / e), "frac_within_3sigma": float(np.mean(np.abs(t) < q)),
+            "mean_t": float(np.mean(t))}
+
+
+def matched_error(V, p, dev, B=10, n_ref=100_000):
+    """B batches of the FP64 CPU oracle (MT19937, all host cores) against B batches of each
+    GPU form; both forms at the same photon count per batch."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    t0 = time.time()
+    ref = []
+    for b in range(B):
+        r = oracle.run(p, rng=oracle.RNG_MT, nthreads=os.cpu_count() or 1, nphoton=n_ref, seed=60000 + 1000 * b)
+        ref.append(np.concatenate([r.ER, r.EBR]))
+    t_ref = time.time() - t0
+    out = {"reference": f"FP64 CPU oracle, {B} batches x {n_ref} photons (MT19937, {os.cpu_count()} threads, "
+                        f"{t_ref:.1f} s)", "batches": B}
+    for prec, name, n in ((V.VMC_FP32, "fp32", 400_000), (V.VMC_FP64, "fp64", 400_000)):
+        mesh = V.Mesh(p, precision=prec, device=dev)
+        rows = []
+        for b in range(B):
+            res, _ = V.run_batch([mesh], [p.copy(Nphoton=n, seed=100 + b)], precision=prec, device=dev)
+            rows.append(np.concatenate([res[0].ER, res[0].EBR]))
+        mesh.close()
+        out[name] = welch_error_to_noise(rows, ref)
+        out[name]["photons_per_batch"] = n
+    out["fp32_over_fp64_error"] = out["fp32"]["error_to_noise"] / out["fp64"]["error_to_noise"]
+    return out
+
+
+# ---------------------------------------------------------------------------------------
+# the other workloads
+# ---------------------------------------------------------------------------------------
+
+def run_fd(args, dev=0):
+    """The frequency-domain phantom (per-tet lognormal mua, U(8, 12) mus, 100 MHz): both forms."""
     import valomc_gb300 as V
     from valomc_gb300 import meshgen as mg
-    rng = np.random.default_rng(seed)
-    sizes = [12, 16, 20, 24]
-    meshes, probs = [], []
-    for L in sizes:
-        p = mg.pencil_box(L, 0.02, 10.0, 0.9, 1.4, (L / 2 + 0.3, L / 2 + 0.2), 1, seed=1)
-        meshes.append(V.Mesh(p))
-        probs.append(p)
-    srv = V.Server(max_slots=64, memory_budget=4 << 30)
-    ids = [srv.add_mesh(m) for m in meshes]
+    p = mg.config_3d_fd(nphoton=int(args.photons), seed=12345)
+    out = {"workload": "FD phantom 648000 tets, f = 100 MHz, lognormal mua, U(8,12) mus"}
+    for prec, name, n, reps in ((V.VMC_FP32, "fp32", int(args.photons), max(1, min(args.steps, 3))),
+                                (V.VMC_FP64, "fp64", int(args.fd_fp64_photons), 1)):
+        mesh = V.Mesh(p, precision=prec, device=dev)
+        q = p.copy(Nphoton=n)
+        V.run_batch([mesh], [q.copy(Nphoton=min(n, 1_000_000))], precision=prec, device=dev)
+        ks, st = [], None
+        for _ in range(reps):
+            flush_l2()
+            _, st = V.run_batch([mesh], [q], precision=prec, device=dev)
+            ks.append(st["seconds_kernel"])
+        k = float(np.median(ks))
+        out[name] = {"photons": n, "photons_per_s": n / k, "tet_steps_per_s": st["steps"] / k,
+                     "steps_per_photon": st["steps"] / n, "achieved_gbs_128B_per_step": BYTES_PER_STEP_FD * st["steps"] / k / 1e9}
+        mesh.close()
+    out["fp32_over_fp64"] = out["fp32"]["photons_per_s"] / out["fp64"]["photons_per_s"]
+    return out
+
+
+def run_square2d(args, dev=0):
+    """The 2D square (10x10 mm, 200 triangles, cosinic source on edges 4..7, 1e6 photons):
+    both forms through vmc_run (host buffers), and the reference's 2D engine on all host
+    cores."""
+    import valomc_gb300 as V
+    from valomc_gb300 import meshgen as mg
+    p = mg.config_2d_square(nphoton=1_000_000, seed=12345)
+    out = {"workload": "10x10 mm square, 200 triangles, cosinic edges 4-7, 1e6 photons"}
+    for prec, name in ((V.VMC_FP64, "fp64"), (V.VMC_FP32, "fp32")):
+        V.run(p, precision=prec, device=dev)
+        rs = [V.run(p, precision=prec, device=dev) for _ in range(max(1, min(args.steps, 5)))]
+        k = float(np.median([r.stats["seconds_kernel"] for r in rs]))
+        tot = float(np.median([r.stats["seconds_total"] for r in rs]))
+        out[name] = {"photons_per_s_kernel": p.Nphoton / k, "photons_per_s_e2e": p.Nphoton / tot,
+                     "steps_per_photon": rs[0].stats["steps"] / p.Nphoton}
+    cb = CpuBaseline(p, "2D square")
+    s, _ = cb.run(p.Nphoton)
+    out["cpu_baseline"] = cb.describe(p.Nphoton, s)
+    for name in ("fp64", "fp32"):
+        out[name]["e2e_over_cpu"] = out[name]["photons_per_s_e2e"] / out["cpu_baseline"]["value"]
+    return out
+
+
+def run_batch_config(args, dev=0):
+    """64 cubes (20-80 mm edges, 48k-3.07M tets each, ~60M in all) with their own optics and
+    pencil sources, photons log-uniform 1e5-1e7, in one persistent launch with the autotuned
+    launch shape, plain and through a CUDA graph."""
+    import valomc_gb300 as V
+    from valomc_gb300 import meshgen as mg
     t0 = time.time()
-    sub = []
-    t = 0.0
-    while t < seconds:
-        t += rng.exponential(1.0 / rate_hz)
-        k = int(rng.integers(len(sizes)))
-        p = probs[k].copy()
-        p.mua[:] = rng.uniform(0.005, 0.1)
-        p.mus[:] = rng.uniform(5, 20)
-        p.g[:] = rng.uniform(0.8, 0.95)
-        p.n[:] = rng.uniform(1.33, 1.45)
-        nph = int(math.exp(rng.uniform(math.log(1e4), math.log(1e6))))
+    probs = mg.config_batch(count=64, photon_scale=args.batch_photon_scale)
+    t_gen = time.time() - t0
+    t0 = time.time()
+    meshes = [V.Mesh(p, device=dev) for p in probs]
+    t_mesh = time.time() - t0
+    tets = sum(p.Ne for p in probs)
+    photons = sum(p.Nphoton for p in probs)
+    t0 = time.time()
+    tuned = V.autotune(meshes, probs, budget_s=args.tune_budget)
+    t_tune = time.time() - t0
+    res = {}
+    for graph in (False, True):
+        o = V.options(block_size=tuned.block_size, blocks_per_sm=tuned.blocks_per_sm, fetch_chunk=tuned.fetch_chunk,
+                      refill_lanes=tuned.refill_lanes, use_graph=graph, device=dev)
+        _, st = V.run_batch(meshes, probs, opts=o)
+        res["graph" if graph else "plain"] = {"kernel_s": st["seconds_kernel"], "wall_s": st["seconds_total"],
+                                              "photons_per_s": photons / st["seconds_kernel"],
+                                              "tet_steps_per_s": st["steps"] / st["seconds_kernel"],
+                                              "steps_per_photon": st["steps"] / photons}
+    _, st = V.run_batch(meshes, probs, device=dev)
+    res["untuned_photons_per_s"] = photons / st["seconds_kernel"]
+    for m in meshes:
+        m.close()
+    return {"workload": "64 cubes L~logU[20,80] mm, pencil sources, config-4 optics, one persistent launch",
+            "photons_per_s": res["graph"]["photons_per_s"], "instances": len(probs), "tets": tets, "photons": photons,
+            "tuned": {"block_size": tuned.block_size, "blocks_per_sm": tuned.blocks_per_sm,
+                      "fetch_chunk": tuned.fetch_chunk, "refill_lanes": tuned.refill_lanes, "tune_s": t_tune},
+            "mesh_gen_s": t_gen, "mesh_upload_s": t_mesh, **res, "photon_scale": args.batch_photon_scale}
+
+
+def run_serve(args, dev=0):
+    """Poisson request stream at --serve-rate over 8 resident cubes (50k-2M tets),
+    cosinic-disk or Gaussian sources at random top points, config-4 optics, photons
+    log-uniform 1e5-1e7, for --serve-window seconds."""
+    import valomc_gb300 as V
+    from valomc_gb300 import meshgen as mg
+    mix = mg.ServingMix(seed=5)
+    meshes = [V.Mesh(b, device=dev) for b in mix.base]
+    srv = V.Server(max_slots=args.serve_slots, memory_budget=16 << 30, epoch_photons=int(args.serve_epoch),
+                   block_size=args.serve_block, device=dev)
+    ids = [srv.add_mesh(m) for m in meshes]
+    k, p = mix.request()
+    srv.wait(srv.submit(ids[k], p.copy(Nphoton=10000)))  # warm the kernels and graphs
+    rng = np.random.default_rng(55)
+    t0 = time.time()
+    t, sub = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / args.serve_rate)
+        if t > args.serve_window:
+            break
+        k, p = mix.request()
         now = time.time() - t0
         if t > now:
             time.sleep(t - now)
-        sub.append((srv.submit(ids[k], p, nphoton=nph, seed=int(rng.integers(1 << 30))), nph, time.time()))
-    lat, tot = [], 0
-    for rid, nph, ts in sub:
+        sub.append((srv.submit(ids[k], p), p.Nphoton))
+    t_sub = time.time() - t0
+    lat, ph, steps = [], 0, 0
+    for rid, n in sub:
         r = srv.wait(rid)
         lat.append(r.stats["seconds_total"])
-        tot += nph
+        ph += n
+        steps += r.stats["steps"]
     wall = time.time() - t0
     srv.close()
-    return {"requests": len(sub), "rate_hz": rate_hz, "p50_s": float(np.percentile(lat, 50)),
-            "p99_s": float(np.percentile(lat, 99)), "photons_per_s": tot / wall,
-            "note": "Poisson arrivals; cubes 12-24 mm, photons log-uniform 1e4-1e6, config-4 optics"}
+    for m in meshes:
+        m.close()
+    offered = sum(n for _, n in sub) / args.serve_window
+    quarter = max(1, len(lat) // 4)
+    q_first, q_last = float(np.median(lat[:quarter])), float(np.median(lat[-quarter:]))
+    return {"workload": "8 cubes 50k-2M tets, cosinic disk / gaussian sources, photons logU[1e5,1e7]",
+            "rate_hz": args.serve_rate, "window_s": args.serve_window, "requests": len(sub),
+            "submit_s": t_sub, "drain_s": wall - t_sub,
+            "offered_photons_per_s": offered, "served_photons_per_s": ph / wall,
+            "served_steps_per_s": steps / wall, "steps_per_photon": steps / max(ph, 1),
+            # stable: the device keeps up (served >= 95% of offered) and the latency does not
+            # grow over the window (median of the last quarter of requests vs the first)
+            "stable": bool(ph / wall >= 0.95 * offered and q_last <= 2.0 * q_first + 0.05),
+            "p50_first_quarter_s": q_first, "p50_last_quarter_s": q_last,
+            "p50_s": float(np.percentile(lat, 50)), "p90_s": float(np.percentile(lat, 90)),
+            "p99_s": float(np.percentile(lat, 99))}
 
+
+# ---------------------------------------------------------------------------------------
+# the headline
+# ---------------------------------------------------------------------------------------
 
 def main():
     ap = argparse.ArgumentParser()
@@ -254,24 +462,30 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--photons", type=float, default=1e8)
     ap.add_argument("--fp64-photons", type=float, default=1e7)
-    ap.add_argument("--ref-seconds", type=float, default=10.0)
+    ap.add_argument("--fd-fp64-photons", type=float, default=2e6)
+    ap.add_argument("--ref-budget", type=float, default=100.0, help="seconds of reference work in --impl reference")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--serve-seconds", type=float, default=6.0)
-    ap.add_argument("--no-extras", action="store_true")
-    ap.add_argument("--config", default="phantom", choices=["phantom", "fd", "batch", "serve", "square2d"],
-                    help="phantom: the headline line; fd / batch / serve: the other workloads, one line each")
+    ap.add_argument("--no-extras", action="store_true", help="the headline numbers only (profiling runs)")
+    ap.add_argument("--config", default="all", choices=["all", "phantom", "fd", "batch", "serve", "square2d"],
+                    help="all: the headline line with every workload; phantom: the headline alone; "
+                         "fd / batch / serve / square2d: one workload, one line")
     ap.add_argument("--batch-photon-scale", type=float, default=1.0)
+    ap.add_argument("--tune-budget", type=float, default=6.0)
     ap.add_argument("--serve-rate", type=float, default=50.0)
     ap.add_argument("--serve-window", type=float, default=10.0)
     ap.add_argument("--serve-epoch", type=float, default=0.0,
-                    help="photons per serving epoch (0: the loop's own choice, 50 ms to 0.5 s of work by backlog)")
+                    help="photons per serving epoch (0: the loop's own choice by backlog)")
     ap.add_argument("--serve-slots", type=int, default=64, help="requests the serving loop simulates at once")
     ap.add_argument("--serve-block", type=int, default=0, help="threads per CTA of the serving launches (0: default)")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
-    if args.config != "phantom":
-        return {"fd": bench_fd, "batch": bench_batch, "serve": bench_serve, "square2d": bench_square2d}[args.config](args)
+    single = {"fd": run_fd, "batch": run_batch_config, "serve": run_serve, "square2d": run_square2d}
+    if args.config in single:
+        out = single[args.config](args)
+        out["config"] = args.config
+        print(json.dumps(out), flush=True)
+        return 0
 
     ws, rank, local = dist_env()
     dist = Dist(ws)
@@ -323,11 +537,11 @@ def main():
     h2d = re.stats["bytes_h2d"]
     d2h = re.stats["bytes_d2h"]
 
-    out = None
     if rank == 0:
         peak, peak_kind = measured_peaks()
         achieved = BYTES_PER_STEP_CW * steps_per_launch / kmean / 1e9
-        traffic_per_step = ncu_traffic()
+        prof = ncu_profile()
+        dram_per_step = prof.get("dram_bytes_per_step")
         line = {
             "metric": METRIC, "value": value, "unit": "photons/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * wall_max / args.steps, "higher_is_better": True,
@@ -341,10 +555,16 @@ def main():
             "kernel_s_per_step": kmean,
             "gpu_launches": args.steps,
             "e2e": {"value": e2e_value, "unit": "photons/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "peak_kind": peak_kind,
-                         "traffic": (traffic_per_step * steps_per_launch) if traffic_per_step else None,
-                         "algorithmic_bytes_per_launch": BYTES_PER_STEP_CW * steps_per_launch},
+            # the kernel is bound by instruction issue (ncu: issue-active, threads per warp
+            # instruction); its memory ceiling is the L2 dependent-gather rate, since the
+            # mesh stays in L2; frac is against the HBM copy peak as the contract has it
+            "roofline": {"bound": "issue", "memory_ceiling": "l2_gather", "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                         "traffic": (dram_per_step * steps_per_launch) if dram_per_step else None,
+                         "algorithmic_bytes_per_launch": BYTES_PER_STEP_CW * steps_per_launch,
+                         "simt_threads_per_inst": prof.get("threads_per_inst"),
+                         "issue_active": prof.get("issue_active"),
+                         "profile": prof.get("kernel")},
             "clocks": clk.summary(),
         }
         if not args.no_extras:
@@ -360,173 +580,22 @@ def main():
             line["fp64"] = {"photons_per_s": fp64_rate, "tet_steps_per_s": r64b.stats["steps"] / r64b.stats["seconds_kernel"],
                             "fp32_over_fp64": fp32_rate / fp64_rate, "fp64_tflops_peak": V.bench_fp64(0.2, dev)}
             line["matched_error"] = matched_error(V, p, dev)
-            line["cpu_baseline"] = cpu_baseline(p, seconds_target=args.cpu_seconds)
+            cb = CpuBaseline(p, "phantom")
+            n_cpu = cb.size_for(args.cpu_seconds)
+            s, _ = cb.run(n_cpu)
+            line["cpu_baseline"] = cb.describe(n_cpu, s)
             line["cpu_baseline"]["gpu_over_cpu"] = value / line["cpu_baseline"]["value"]
-            if args.serve_seconds > 0:
-                line["serve"] = serve_run(args.serve_seconds, 50.0)
-        out = line
-        print(json.dumps(out), flush=True)
+            line["cpu_baseline"]["e2e_over_cpu"] = e2e_value / line["cpu_baseline"]["value"]
+            mesh.close()
+            line["configs"] = {}
+            for name, fn in (("square2d", run_square2d), ("fd", run_fd), ("batch", run_batch_config),
+                             ("serve", run_serve)):
+                t0 = time.time()
+                line["configs"][name] = fn(args, dev)
+                line["configs"][name]["bench_s"] = time.time() - t0
+        print(json.dumps(line), flush=True)
     dist.close()
     return 0
-
-
-def bench_fd(args):
-    """The frequency-domain phantom (per-tet lognormal mua, U(8, 12) mus, 100 MHz): both forms."""
-    import valomc_gb300 as V
-    from valomc_gb300 import meshgen as mg
-    p = mg.config_3d_fd(nphoton=int(args.photons), seed=12345)
-    out = {"metric": "photons/s, frequency-domain phantom", "unit": "photons/s",
-           "config": {"workload": "FD phantom 648000 tets, f = 100 MHz, lognormal mua, U(8,12) mus"}}
-    for prec, name, n in ((V.VMC_FP32, "fp32", int(args.photons)), (V.VMC_FP64, "fp64", int(args.fp64_photons))):
-        mesh = V.Mesh(p, precision=prec)
-        q = p.copy(Nphoton=n)
-        V.run_batch([mesh], [q], precision=prec)
-        ks, st = [], None
-        for _ in range(max(1, args.steps)):
-            flush_l2()
-            _, st = V.run_batch([mesh], [q], precision=prec)
-            ks.append(st["seconds_kernel"])
-        k = float(np.median(ks))
-        out[name] = {"photons_per_s": n / k, "tet_steps_per_s": st["steps"] / k, "steps_per_photon": st["steps"] / n,
-                     "achieved_gbs_128B_per_step": 128 * st["steps"] / k / 1e9}
-        mesh.close()
-    out["value"] = out["fp32"]["photons_per_s"]
-    out["fp32_over_fp64"] = out["fp32"]["photons_per_s"] / out["fp64"]["photons_per_s"]
-    print(json.dumps(out), flush=True)
-    return 0
-
-
-def bench_square2d(args):
-    """The 2D square (10x10 mm, 200 triangles, cosinic source on edges 4..7, 1e6 photons):
-    both forms through vmc_run (host buffers), and the CPU oracle on all host cores."""
-    import valomc_gb300 as V
-    from valomc_gb300 import meshgen as mg
-    p = mg.config_2d_square(nphoton=1_000_000, seed=12345)
-    out = {"metric": "photons/s, 2D square", "unit": "photons/s",
-           "config": {"workload": "10x10 mm square, 200 triangles, cosinic edges 4-7, 1e6 photons"}}
-    for prec, name in ((V.VMC_FP64, "fp64"), (V.VMC_FP32, "fp32")):
-        V.run(p, precision=prec)
-        rs = [V.run(p, precision=prec) for _ in range(max(1, args.steps))]
-        k = min(r.stats["seconds_kernel"] for r in rs)
-        tot = min(r.stats["seconds_total"] for r in rs)
-        out[name] = {"photons_per_s_kernel": p.Nphoton / k, "photons_per_s_e2e": p.Nphoton / tot,
-                     "steps_per_photon": rs[0].stats["steps"] / p.Nphoton}
-    out["cpu_baseline"] = cpu_baseline(p, seconds_target=5.0, name="2D square")
-    out["value"] = out["fp64"]["photons_per_s_e2e"]
-    print(json.dumps(out), flush=True)
-    return 0
-
-
-def bench_batch(args):
-    """64 cubes (20-80 mm edges, 48k-3.07M tets each, ~46M in all) with their own optics and
-    pencil sources, photons log-uniform 1e5-1e7, in one persistent launch with the autotuned
-    launch shape, plain and through a CUDA graph."""
-    import valomc_gb300 as V
-    from valomc_gb300 import meshgen as mg
-    t0 = time.time()
-    probs = mg.config_batch(count=64, photon_scale=args.batch_photon_scale)
-    t_gen = time.time() - t0
-    t0 = time.time()
-    meshes = [V.Mesh(p) for p in probs]
-    t_mesh = time.time() - t0
-    tets = sum(p.Ne for p in probs)
-    photons = sum(p.Nphoton for p in probs)
-    t0 = time.time()
-    tuned = V.autotune(meshes, probs, budget_s=6.0)
-    t_tune = time.time() - t0
-    res = {}
-    for graph in (False, True):
-        o = V.options(block_size=tuned.block_size, blocks_per_sm=tuned.blocks_per_sm, fetch_chunk=tuned.fetch_chunk,
-                      use_graph=graph)
-        _, st = V.run_batch(meshes, probs, opts=o)
-        res["graph" if graph else "plain"] = {"kernel_s": st["seconds_kernel"], "wall_s": st["seconds_total"],
-                                              "photons_per_s": photons / st["seconds_kernel"],
-                                              "tet_steps_per_s": st["steps"] / st["seconds_kernel"],
-                                              "steps_per_photon": st["steps"] / photons}
-    dflt, st = V.run_batch(meshes, probs)
-    res["untuned_photons_per_s"] = photons / st["seconds_kernel"]
-    out = {"metric": "photons/s, 64 batched instances in one persistent launch", "unit": "photons/s",
-           "value": res["graph"]["photons_per_s"], "instances": len(probs), "tets": tets, "photons": photons,
-           "tuned": {"block_size": tuned.block_size, "blocks_per_sm": tuned.blocks_per_sm,
-                     "fetch_chunk": tuned.fetch_chunk, "tune_s": t_tune},
-           "mesh_gen_s": t_gen, "mesh_upload_s": t_mesh,
-           "device_mesh_bytes": int(sum(m.device_bytes for m in meshes)), **res,
-           "config": {"workload": "64 cubes L~logU[20,80] mm, pencil sources, config-4 optics",
-                      "photon_scale": args.batch_photon_scale}}
-    print(json.dumps(out), flush=True)
-    return 0
-
-
-def bench_serve(args):
-    """Poisson request stream over 8 resident cubes (50k-2M tets), cosinic-disk or Gaussian
-    sources at random top points, config-4 optics, photons log-uniform 1e5-1e7."""
-    import valomc_gb300 as V
-    from valomc_gb300 import meshgen as mg
-    mix = mg.ServingMix(seed=5)
-    meshes = [V.Mesh(b) for b in mix.base]
-    srv = V.Server(max_slots=args.serve_slots, memory_budget=16 << 30, epoch_photons=int(args.serve_epoch),
-                   block_size=args.serve_block)
-    ids = [srv.add_mesh(m) for m in meshes]
-    # warm the kernels and graphs
-    k, p = mix.request()
-    srv.wait(srv.submit(ids[k], p.copy(Nphoton=10000)))
-    rng = np.random.default_rng(55)
-    t0 = time.time()
-    t, sub = 0.0, []
-    while True:
-        t += rng.exponential(1.0 / args.serve_rate)
-        if t > args.serve_window:
-            break
-        k, p = mix.request()
-        now = time.time() - t0
-        if t > now:
-            time.sleep(t - now)
-        sub.append((srv.submit(ids[k], p), p.Nphoton))
-    t_sub = time.time() - t0
-    lat, ph, steps = [], 0, 0
-    for rid, n in sub:
-        r = srv.wait(rid)
-        lat.append(r.stats["seconds_total"])
-        ph += n
-        steps += r.stats["steps"]
-    wall = time.time() - t0
-    srv.close()
-    offered = sum(n for _, n in sub) / args.serve_window
-    quarter = max(1, len(lat) // 4)
-    q_first, q_last = float(np.median(lat[:quarter])), float(np.median(lat[-quarter:]))
-    out = {"metric": "serve p50/p99 latency and photons/s", "unit": "s", "rate_hz": args.serve_rate,
-           "window_s": args.serve_window, "epoch_photons": int(args.serve_epoch), "slots": args.serve_slots,
-           "block_size": args.serve_block, "requests": len(sub),
-           "submit_s": t_sub, "drain_s": wall - t_sub,
-           "offered_photons_per_s": offered, "served_photons_per_s": ph / wall,
-           "served_steps_per_s": steps / wall, "steps_per_photon": steps / max(ph, 1),
-           # stable: the device keeps up (served >= 95% of offered) and the latency does not
-           # grow over the window (median of the last quarter of requests vs the first)
-           "stable": bool(ph / wall >= 0.95 * offered and q_last <= 2.0 * q_first + 0.05),
-           "p50_first_quarter_s": q_first, "p50_last_quarter_s": q_last,
-           "p50_s": float(np.percentile(lat, 50)), "p90_s": float(np.percentile(lat, 90)),
-           "p99_s": float(np.percentile(lat, 99)), "value": float(np.percentile(lat, 99)),
-           "config": {"workload": "8 cubes 50k-2M tets, cosinic disk / gaussian sources, photons logU[1e5,1e7]"}}
-    print(json.dumps(out), flush=True)
-    return 0
-
-
-def matched_error(V, p, dev, B=10, n=400000):
-    """chi2/dof of per-element batch means, FP32 form vs FP64 form, same photon count."""
-    def bm(prec, base):
-        xs = np.stack([V.run(p, precision=prec, device=dev, nphoton=n, seed=base + b).ER for b in range(B)])
-        return xs.mean(0), xs.std(0, ddof=1) / math.sqrt(B), np.all(xs > 0, axis=0)
-    m32, s32, h32 = bm(V.VMC_FP32, 100)
-    m64, s64, h64 = bm(V.VMC_FP64, 900)
-    hit = h32 & h64
-    z = (m32[hit] - m64[hit]) / np.sqrt(s32[hit] ** 2 + s64[hit] ** 2)
-    # ratio of FP32 error to the noise floor: sqrt of the mean squared z over 1 for an
-    # unbiased estimator whose noise equals the FP64 form's
-    rel32 = np.median(s32[hit] / m32[hit])
-    rel64 = np.median(s64[hit] / m64[hit])
-    return {"chi2_per_dof": float(np.mean(z ** 2)), "frac_within_3sigma": float(np.mean(np.abs(z) < 3)),
-            "elements": int(hit.sum()), "noise_ratio_fp32_over_fp64": float(rel32 / rel64),
-            "batches": B, "photons_per_batch": n}
 
 
 if __name__ == "__main__":
