@@ -260,32 +260,42 @@ def reference_arm(args):
 # matched error: each GPU form against the FP64 CPU oracle, per element
 # ---------------------------------------------------------------------------------------
 
-def welch_error_to_noise(gpu_rows, ref_rows, rel=0.05):
-    """Over elements whose batch means have a relative standard error below `rel` on both
-    sides: chi2/dof of the Welch t statistics, its t-expectation mean(nu / (nu - 2)), the
-    fraction within the 3-sigma t quantile, and the error-to-noise ratio
-    sqrt(chi2 / expectation) (1: the GPU form's error is the Monte Carlo noise)."""
-    from scipy.stats import t as student_t
-    g, r = np.asarray(gpu_rows), np.asarray(ref_rows)
+def _welch(g, r, sel):
     Bg, Br = len(g), len(r)
-    gm, gv = g.mean(0), g.var(0, ddof=1) / Bg
-    rm, rv = r.mean(0), r.var(0, ddof=1) / Br
-    ok = np.all(g != 0, axis=0) & np.all(r != 0, axis=0)
-    ok[ok] = (np.sqrt(gv[ok]) < rel * np.abs(gm[ok])) & (np.sqrt(rv[ok]) < rel * np.abs(rm[ok]))
-    s2 = gv[ok] + rv[ok]
-    t = (gm[ok] - rm[ok]) / np.sqrt(s2)
-    nu = s2 ** 2 / (gv[ok] ** 2 / (Bg - 1) + rv[ok] ** 2 / (Br - 1))
-    e = float(np.mean(nu / (nu - 2)))
-    chi2 = float(np.mean(t * t))
+    gm, gv = g.mean(0)[sel], g.var(0, ddof=1)[sel] / Bg
+    rm, rv = r.mean(0)[sel], r.var(0, ddof=1)[sel] / Br
+    s2 = gv + rv
+    t = (gm - rm) / np.sqrt(s2)
+    nu = s2 ** 2 / (gv ** 2 / (Bg - 1) + rv ** 2 / (Br - 1))
+    return t, nu
+
+
+def welch_error_to_noise(gpu_rows, ref_rows, null_rows, rel=0.05):
+    """Over elements whose batch means have a relative standard error below `rel` on every
+    side: chi2/dof of the Welch t statistics of the GPU batches against the oracle's, and
+    against independent GPU batches of the oracle's size (the noise floor: the value the
+    comparison takes when the GPU form is distributed exactly as the oracle), and
+    error_to_noise = sqrt(chi2 / chi2 of the noise floor).  chi2/dof of an exact match
+    exceeds the t-expectation mean(nu / (nu - 2)) because batch means of tallies are
+    skewed; both are reported."""
+    from scipy.stats import t as student_t
+    g, r, n = np.asarray(gpu_rows), np.asarray(ref_rows), np.asarray(null_rows)
+    ok = np.all(g != 0, axis=0) & np.all(r != 0, axis=0) & np.all(n != 0, axis=0)
+    for x in (g, r, n):
+        ok[ok] &= x.std(0, ddof=1)[ok] / math.sqrt(len(x)) < rel * np.abs(x.mean(0)[ok])
+    t, nu = _welch(g, r, ok)
+    tn, _ = _welch(g, n, ok)
+    chi2, chi2n = float(np.mean(t * t)), float(np.mean(tn * tn))
     q = student_t.ppf(0.5 + 0.99730020393674 / 2, nu)
-    return {"elements": int(ok.sum()), "chi2_per_dof": chi2, "t_expectation": e,
-            "error_to_noise": math.sqrt(chi2 / e), "frac_within_3sigma": float(np.mean(np.abs(t) < q)),
-            "mean_t": float(np.mean(t))}
+    return {"elements": int(ok.sum()), "chi2_per_dof": chi2, "noise_floor_chi2_per_dof": chi2n,
+            "t_expectation": float(np.mean(nu / (nu - 2))), "error_to_noise": math.sqrt(chi2 / chi2n),
+            "frac_within_3sigma": float(np.mean(np.abs(t) < q)), "mean_t": float(np.mean(t))}
 
 
 def matched_error(V, p, dev, B=10, n_ref=100_000):
     """B batches of the FP64 CPU oracle (MT19937, all host cores) against B batches of each
-    GPU form; both forms at the same photon count per batch."""
+    GPU form (both forms at the same photon count per batch), with B more GPU batches of
+    the oracle's size for the noise floor."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     oracle.build()
@@ -299,13 +309,15 @@ def matched_error(V, p, dev, B=10, n_ref=100_000):
                         f"{t_ref:.1f} s)", "batches": B}
     for prec, name, n in ((V.VMC_FP32, "fp32", 400_000), (V.VMC_FP64, "fp64", 400_000)):
         mesh = V.Mesh(p, precision=prec, device=dev)
-        rows = []
-        for b in range(B):
-            res, _ = V.run_batch([mesh], [p.copy(Nphoton=n, seed=100 + b)], precision=prec, device=dev)
-            rows.append(np.concatenate([res[0].ER, res[0].EBR]))
-        mesh.close()
-        out[name] = welch_error_to_noise(rows, ref)
+
+        def rows(count, seed0):
+            res = [V.run_batch([mesh], [p.copy(Nphoton=count, seed=seed0 + b)], precision=prec, device=dev)[0][0]
+                   for b in range(B)]
+            return [np.concatenate([x.ER, x.EBR]) for x in res]
+
+        out[name] = welch_error_to_noise(rows(n, 100), ref, rows(n_ref, 500))
         out[name]["photons_per_batch"] = n
+        mesh.close()
     out["fp32_over_fp64_error"] = out["fp32"]["error_to_noise"] / out["fp64"]["error_to_noise"]
     return out
 

@@ -232,7 +232,8 @@ typedef struct vmc_server_config {
   int32_t precision;
   int32_t max_slots;          /* requests simulated concurrently */
   int32_t use_graph;          /* run each epoch's launches as an updated CUDA graph */
-  int64_t memory_budget;      /* bytes of per-request device state admitted at once */
+  int64_t memory_budget;      /* bytes of per-request device state admitted at once; clamped
+                                 to the device's free memory (less 256 MiB) at creation */
   int64_t epoch_photons;      /* photons per launch across all slots; 0 = by load: 50 ms of
                                  work at the measured rate while the backlog is small, up to
                                  the backlog and 0.5 s of work as it grows */

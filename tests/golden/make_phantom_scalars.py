@@ -86,9 +86,10 @@ def main():
     rows_r, rows_i, secs = [], [], []
     for b in range(B):
         t0 = time.time()
-        # thread t of a reference run draws from MT seed seed * threads + t: seeds 90000 + b
-        # keep every batch's streams apart
-        out = oracle.ref_run(p.copy(seed=90000 + b), nthreads=threads)
+        # thread t of a reference run draws from MT seed (seed + t) (MonteCarlo seeds thread t
+        # with seed * totalthreads + t, cpp/3d/MC3D.hpp:1658, and totalthreads is 1 without
+        # MPI): seeds 1000 apart keep every batch's streams apart
+        out = oracle.ref_run(p.copy(seed=90000 + 1000 * b), nthreads=threads)
         assert out["status"] == 0
         rows_r.append(apply(W, out["ER"], out["EBR"]))
         rows_i.append(apply(W, out["EI"], out["EBI"]))
@@ -97,7 +98,7 @@ def main():
     name = "phantom_scalars.npz" if kind == "cw" else "phantom_fd_scalars.npz"
     np.savez_compressed(os.path.join(HERE, name), names=np.array(W[0]), real=np.array(rows_r), imag=np.array(rows_i),
                         photons=n, threads=threads, seconds=np.array(secs),
-                        engine="reference MonteCarlo() (oracle/_ref/ref3d_run), MT19937, seeds 90000 + batch")
+                        engine="reference MonteCarlo() (oracle/_ref/ref3d_run), MT19937, seeds 90000 + 1000 batch")
 
 
 if __name__ == "__main__":

@@ -19,7 +19,7 @@ import pytest
 import oracle
 import valomc_gb300 as V
 from golden.make_golden import TRACE_CASES, cases, tape_for
-from parity_stats import Batches, chi2_excess_ok, element_report, fmt
+from parity_stats import Batches, chi2_excess_ok, element_report, fmt, mean_t_ok, within3_ok
 from valomc_gb300 import meshgen as mg
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
@@ -129,9 +129,9 @@ def test_fluence_within_batch_means_error_of_oracle(built, name, precision):
     print(fmt(label, rep))
     h, w = rep["hit"], rep["well"]
     assert h["n"] > 50, (label, rep)
-    assert h["within3"] >= 0.985 and chi2_excess_ok(h), (label, rep)
+    assert within3_ok(h, 0.985) and chi2_excess_ok(h), (label, rep)
     if w["n"] >= 200:  # enough near-Gaussian elements for the strict gate
-        assert w["within3"] >= 0.99 and w["within3"] >= w["null"]["within3"] - 0.003 and chi2_excess_ok(w), (label, rep)
+        assert within3_ok(w, 0.99) and chi2_excess_ok(w) and mean_t_ok(w), (label, rep)
 
 
 @pytest.mark.parametrize("precision", [V.VMC_FP64, V.VMC_FP32])

@@ -353,6 +353,17 @@ int vmc_server_create(const vmc_server_config *cfg, vmc_server **out) {
   vmc_server *sv = new vmc_server;
   sv->cfg = *cfg;
   {
+    // admission cannot promise more device memory than the device has free: the budget is
+    // clamped to the free bytes at creation, less a margin for the launch tables and the
+    // stream-ordered pool's own granularity
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
+      const int64_t margin = 256ll << 20;
+      const int64_t usable = std::max<int64_t>(0, (int64_t)free_b - margin);
+      if (sv->cfg.memory_budget > usable) sv->cfg.memory_budget = usable;
+    }
+  }
+  {
     cudaMemPoolProps props;
     memset(&props, 0, sizeof(props));
     props.allocType = cudaMemAllocationTypePinned;
