@@ -109,14 +109,16 @@ struct Walk2D64 {
     double norm = sqrt(ddx * ddx + ddy * ddy);
     nor[0] = ddy / norm; nor[1] = -ddx / norm;
   }
-  // Edge f runs from vertex f to vertex f + 1 (mod 3); constant indices in each case keep
-  // the vertex array in registers (an index computed from f would put it in local memory).
-  __device__ __forceinline__ static void edge_normal(const double V[3][2], int f, double nor[2]) {
-    switch (f) {
-      case 0: normal_of(V[0], V[1], nor); break;
-      case 1: normal_of(V[1], V[2], nor); break;
-      default: normal_of(V[2], V[0], nor); break;
-    }
+  // Edge f runs from vertex f to vertex f + 1 (mod 3).  Only the Fresnel and exit paths
+  // need its normal, so they read the two vertices again from the element record (the same
+  // doubles) instead of indexing the step's vertex array by f, which would put that array
+  // in local memory for the whole step.
+  __device__ static void edge_normal(const Tri64 *T, int f, double nor[2]) {
+    const double *v = &T->v[0][0];
+    const int i0 = f, i1 = f == 2 ? 0 : f + 1;
+    const double a[2] = {__ldg(v + 2 * i0), __ldg(v + 2 * i0 + 1)};
+    const double b[2] = {__ldg(v + 2 * i1), __ldg(v + 2 * i1 + 1)};
+    normal_of(a, b, nor);
   }
 
   __device__ bool roulette(const JobDev &J, R &rng) {
@@ -199,7 +201,7 @@ struct Walk2D64 {
         return kAlive;
       }
       double nor[2];
-      edge_normal(V, nf, nor);
+      edge_normal(T, nf, nor);
       const double bcn = __ldg(J.bcn + ib);
       if (bcn > 0.0 && fresnel(rng, nor, nidx / bcn, nf, true)) return kAlive;
       // outward edge normal for DEBR (MC2D.hpp:1410-1423)
@@ -232,14 +234,14 @@ struct Walk2D64 {
       if (roulette(J, rng)) return die(J, kEvRoulette);
       if (nidx != n2) {
         double nor[2];
-        edge_normal(V, nf, nor);
+        edge_normal(T, nf, nor);
         if (fresnel(rng, nor, nidx / n2, nf, false)) return kAlive;
       }
     } else {
       if (roulette(J, rng)) return die(J, kEvRoulette);
       if (nidx != n2) {
         double nor[2];
-        edge_normal(V, nf, nor);
+        edge_normal(T, nf, nor);
         if (fresnel(rng, nor, nidx / n2, nf, false)) return kAlive;
       }
       if (mus2 != mus) prop *= mus / mus2;  // x (mus / mus) == x: skip the division
@@ -401,12 +403,13 @@ struct Walk2D32 {
     {
       const float4 ln[3] = {l0, l1, l2};
 #pragma unroll
-      for (int f = 0; f < 3; f++) {
-        float nd = ln[f].x * dx + ln[f].y * dy;
-        if (nd > 0.0f) {
-          float t = __fdividef(ln[f].z - (ln[f].x * px + ln[f].y * py), nd);
-          if (t < best) { best = t; nf = f; }
-        }
+      for (int f = 0; f < 3; f++) {  // selects over all three edges, no branch per edge
+        const float nd = ln[f].x * dx + ln[f].y * dy;
+        const float num = ln[f].z - (ln[f].x * px + ln[f].y * py);
+        const float t = nd > 0.0f ? __fdividef(num, nd) : INFINITY;
+        const bool better = t < best;
+        best = better ? t : best;
+        nf = better ? f : nf;
       }
     }
     if (nf < 0) {
@@ -484,6 +487,15 @@ struct Walk2D32 {
       return die(J, kEvLost);
     }
     const float4 o2 = optics(J, nextel);
+    // the common crossing (scattering medium, weight above the roulette threshold, no index
+    // jump) tested at once
+    if (mus > 0.0f && w >= (float)kWeight0 && nidx == o2.w) {
+      if (o2.y != mus) prop *= mus / o2.y;
+      flush(J);
+      el = nextel;
+      mua = o2.x; mus = o2.y; g = o2.z; nidx = o2.w;
+      return kAlive;
+    }
     if (mus <= 0.0f && o2.y > 0.0f) {
       prop = free_path_f(unif_open_f(rng), o2.y);
       if (roulette(J, rng)) return die(J, kEvRoulette);

@@ -29,13 +29,8 @@ __device__ __forceinline__ bool ray_tri(const double O[3], const double D[3], co
   double det = e1[0] * pv[0] + e1[1] * pv[1] + e1[2] * pv[2];
   if ((-kDblEps < det) && (det < kDblEps)) return false;
   double tv[3] = {O[0] - V0[0], O[1] - V0[1], O[2] - V0[2]};
-  const double du = tv[0] * pv[0] + tv[1] * pv[1] + tv[2] * pv[2];
-  // u = du / det < 0 exactly when du and det have opposite signs (their product cannot
-  // round to zero: |du| is far above 2^-1074 |det| for any nonzero coordinate
-  // differences), so that half of the rejections is decided before the division
-  if ((du < 0.0) != (det < 0.0) && du != 0.0) return false;
   double inv = 1.0 / det;
-  double u = du * inv;
+  double u = (tv[0] * pv[0] + tv[1] * pv[1] + tv[2] * pv[2]) * inv;
   if ((u < 0.0) || (u > 1.0)) return false;
   double qv[3] = {tv[1] * e1[2] - tv[2] * e1[1], tv[2] * e1[0] - tv[0] * e1[2], tv[0] * e1[1] - tv[1] * e1[0]};
   double v = (D[0] * qv[0] + D[1] * qv[1] + D[2] * qv[2]) * inv;
@@ -88,9 +83,9 @@ __device__ __forceinline__ bool is_mirror(uint8_t bt) { return bt == 'm' || bt =
 // (truncation x^6/720, relative x^5/720 < 1.4e-8); above, 1 - exp(-x) from the fast
 // exponential (relative error < 2^-22 / (1 - e^-0.1) ~ 1.3e-6 at the cut, falling beyond).
 __device__ __forceinline__ float one_minus_exp_neg(float x) {
-  if (x < 0.1f)
-    return x * (1.0f + x * (-0.5f + x * (1.0f / 6.0f + x * (-1.0f / 24.0f + x * (1.0f / 120.0f)))));
-  return 1.0f - __expf(-x);
+  const float s = x * (1.0f + x * (-0.5f + x * (1.0f / 6.0f + x * (-1.0f / 24.0f + x * (1.0f / 120.0f)))));
+  const float e = 1.0f - __expf(-x);
+  return x < 0.1f ? s : e;  // a select, not a branch
 }
 
 // sin(t) for the per-step phase increments of the frequency-domain walk (|t| ~ 1e-3): the
@@ -361,16 +356,16 @@ struct Walk3D64 {
     double norm = sqrt(nx * nx + ny * ny + nz * nz);
     nor[0] = nx / norm; nor[1] = ny / norm; nor[2] = nz / norm;
   }
-  // Face f of the tetrahedron is (0,1,2), (0,1,3), (0,2,3) or (1,2,3).  Each case names its
-  // vertices with constant indices, so the vertex array stays in registers (an index
-  // computed from f would put it in local memory for the whole step).
+  // Face f of the tetrahedron is (0,1,2), (0,1,3), (0,2,3) or (1,2,3).  The index computed
+  // from f puts the step's vertex array in local memory (an L1-resident store of 96 B per
+  // step); keeping it in registers to the end of the step (constant indices per case), or
+  // reading the vertices again on the Fresnel paths, takes more registers, halves the
+  // resident CTAs and measured 5-15 % slower on the phantom, whose FP64 pipe is the bound.
   __device__ __forceinline__ static void face_normal(const double V[4][3], int f, double nor[3]) {
-    switch (f) {
-      case 0: normal_of(V[0], V[1], V[2], nor); break;
-      case 1: normal_of(V[0], V[1], V[3], nor); break;
-      case 2: normal_of(V[0], V[2], V[3], nor); break;
-      default: normal_of(V[1], V[2], V[3], nor); break;
-    }
+    const int i0 = f == 3 ? 1 : 0;
+    const int i1 = f == 0 ? 1 : f == 1 ? 1 : 2;
+    const int i2 = f == 0 ? 2 : 3;
+    normal_of(V[i0], V[i1], V[i2], nor);
   }
 };
 
@@ -528,18 +523,20 @@ struct Walk3D32 {
     const float4 *P4 = reinterpret_cast<const float4 *>(T->pl);
     const float4 p0 = __ldg(P4 + 0), p1 = __ldg(P4 + 1), p2 = __ldg(P4 + 2), p3 = __ldg(P4 + 3);
     const int4 nb = __ldg(reinterpret_cast<const int4 *>(T->nbr));
-    // exit: nearest face the direction points out of
+    // exit: nearest face the direction points out of, as selects over all four faces (no
+    // branch per face: fewer divergent regions and 6 fewer registers)
     float best = INFINITY;
     int nf = -1;
     {
       const float4 pl[4] = {p0, p1, p2, p3};
 #pragma unroll
       for (int f = 0; f < 4; f++) {
-        float nd = pl[f].x * dx + pl[f].y * dy + pl[f].z * dz;
-        if (nd > 0.0f) {
-          float t = __fdividef(pl[f].w - (pl[f].x * px + pl[f].y * py + pl[f].z * pz), nd);
-          if (t < best) { best = t; nf = f; }
-        }
+        const float nd = pl[f].x * dx + pl[f].y * dy + pl[f].z * dz;
+        const float num = pl[f].w - (pl[f].x * px + pl[f].y * py + pl[f].z * pz);
+        const float t = nd > 0.0f ? __fdividef(num, nd) : INFINITY;
+        const bool better = t < best;
+        best = better ? t : best;
+        nf = better ? f : nf;
       }
     }
     if (nf < 0) {
@@ -617,6 +614,15 @@ struct Walk3D32 {
       tr.put(-1 - (int64_t)ib);
       tr.end();
       return kDied;
+    }
+    // the common crossing (interior, scattering medium, weight above the roulette
+    // threshold, no index jump) tested at once
+    if (nextel < J.Ne && mus > 0.0f && w >= (float)kWeight0 && nidx == o2.w) {
+      if (o2.y != mus) prop *= mus / o2.y;
+      flush(J);
+      el = nextel;
+      mua = o2.x; mus = o2.y; g = o2.z; nidx = o2.w;
+      return kAlive;
     }
     if (nextel >= J.Ne) {
       job_count(J, kJcLoss); job_ledger(J, kLgLost, f2d_int(w));
