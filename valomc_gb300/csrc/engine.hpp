@@ -114,12 +114,13 @@ int launch_finish(LaunchArena &a, cudaStream_t st, LaunchResult &res);
 int collect_job(const HostJob &j, const DeviceMesh &m, const JobBuffers &b, int64_t nphoton, bool normalize,
                 vmc_output *out, vmc_stats *st, cudaStream_t stream);
 
-const void *kernel_3d64(bool fd, bool tape, bool one);
-const void *kernel_3d32(bool fd, bool tape, bool one);
-const void *kernel_2d64(bool fd, bool tape, bool one);
-const void *kernel_2d32(bool fd, bool tape, bool one);
-// one: the single-job form (descriptor and round keys in LaunchParams::job0 / rk)
-const void *select_kernel(const LaunchSpec &s, bool one = false);
+const void *kernel_3d64(bool fd, bool tape, bool one, bool tab);
+const void *kernel_3d32(bool fd, bool tape, bool one, bool tab);
+const void *kernel_2d64(bool fd, bool tape, bool one, bool tab);
+const void *kernel_2d32(bool fd, bool tape, bool one, bool tab);
+// one: the single-job form (descriptor and round keys in LaunchParams::job0 / rk);
+// tab: the per-job form with the job table copied into each CTA's shared memory
+const void *select_kernel(const LaunchSpec &s, bool one = false, bool tab = false);
 void set_single_job(LaunchParams &lp, const JobDev &job);
 
 }  // namespace vmc

@@ -6,15 +6,18 @@
 
 namespace vmc {
 
-const void *kernel_2d32(bool fd, bool tape, bool one) {
-  if (fd) {
-    if (tape) return reinterpret_cast<const void *>(&pool_kernel<Walk2D32<true, TapeRng>, TapeRng>);
-    if (one) return reinterpret_cast<const void *>(&pool_kernel<Walk2D32<true, PhiloxOne>, PhiloxOne>);
-    return reinterpret_cast<const void *>(&pool_kernel<Walk2D32<true, PhiloxRng>, PhiloxRng>);
-  }
-  if (tape) return reinterpret_cast<const void *>(&pool_kernel<Walk2D32<false, TapeRng>, TapeRng>);
-  if (one) return reinterpret_cast<const void *>(&pool_kernel<Walk2D32<false, PhiloxOne>, PhiloxOne>);
-  return reinterpret_cast<const void *>(&pool_kernel<Walk2D32<false, PhiloxRng>, PhiloxRng>);
+namespace {
+template <class F> const void *K(F *f) { return reinterpret_cast<const void *>(f); }
+template <bool FD, class R> const void *per_job(bool tab) {
+  return tab ? K(&pool_kernel<Walk2D32<FD, R>, R, true>) : K(&pool_kernel<Walk2D32<FD, R>, R, false>);
+}
+}  // namespace
+
+const void *kernel_2d32(bool fd, bool tape, bool one, bool tab) {
+  if (one) return fd ? K(&pool_kernel<Walk2D32<true, PhiloxOne>, PhiloxOne, false>)
+                     : K(&pool_kernel<Walk2D32<false, PhiloxOne>, PhiloxOne, false>);
+  if (tape) return fd ? per_job<true, TapeRng>(tab) : per_job<false, TapeRng>(tab);
+  return fd ? per_job<true, PhiloxRng>(tab) : per_job<false, PhiloxRng>(tab);
 }
 
 }  // namespace vmc

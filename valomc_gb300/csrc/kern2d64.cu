@@ -5,13 +5,16 @@
 
 namespace vmc {
 
-const void *kernel_2d64(bool fd, bool tape, bool /*one: FP32 walks only*/) {
-  if (fd) {
-    if (tape) return reinterpret_cast<const void *>(&pool_kernel<Walk2D64<true, TapeRng>, TapeRng>);
-    return reinterpret_cast<const void *>(&pool_kernel<Walk2D64<true, PhiloxRng>, PhiloxRng>);
-  }
-  if (tape) return reinterpret_cast<const void *>(&pool_kernel<Walk2D64<false, TapeRng>, TapeRng>);
-  return reinterpret_cast<const void *>(&pool_kernel<Walk2D64<false, PhiloxRng>, PhiloxRng>);
+namespace {
+template <class F> const void *K(F *f) { return reinterpret_cast<const void *>(f); }
+template <bool FD, class R> const void *per_job(bool tab) {
+  return tab ? K(&pool_kernel<Walk2D64<FD, R>, R, true>) : K(&pool_kernel<Walk2D64<FD, R>, R, false>);
+}
+}  // namespace
+
+const void *kernel_2d64(bool fd, bool tape, bool /*one: FP32 walks only*/, bool tab) {
+  if (tape) return fd ? per_job<true, TapeRng>(tab) : per_job<false, TapeRng>(tab);
+  return fd ? per_job<true, PhiloxRng>(tab) : per_job<false, PhiloxRng>(tab);
 }
 
 }  // namespace vmc

@@ -22,11 +22,12 @@ __device__ __forceinline__ void start_rng(TapeRng &rng, const JobDev &J, int64_t
   rng.start_tape(J.tape + J.tape_off[q], J.tape + J.tape_off[q + 1]);
 }
 
-__device__ __forceinline__ int find_job(const LaunchParams &lp, int64_t p) {
-  int lo = 0, hi = lp.njobs - 1;
+// the job whose photon range [begin[j], begin[j + 1]) holds photon p
+__device__ __forceinline__ int find_job(const int64_t *begin, int njobs, int64_t p) {
+  int lo = 0, hi = njobs - 1;
   while (lo < hi) {
     int mid = (lo + hi + 1) >> 1;
-    if (__ldg(lp.job_begin + mid) <= p) lo = mid;
+    if (begin[mid] <= p) lo = mid;
     else hi = mid - 1;
   }
   return lo;
@@ -34,13 +35,32 @@ __device__ __forceinline__ int find_job(const LaunchParams &lp, int64_t p) {
 
 // R::kOneJob: a launch of one job, whose descriptor (lp.job0) and Philox round keys are read
 // from the kernel parameters (constant bank) rather than from global memory and registers.
-template <class W, class R>
+// kTab: a launch of at most kSmemJobs jobs whose CTAs first copy the job table and its
+// photon prefix into shared memory, so that the walk reads the descriptor of each lane's
+// job there instead of from global memory (the table follows the dynamic shared memory's
+// start; multi-job launches stage no accumulators).
+template <class W, class R, bool kTab>
 __global__ void __launch_bounds__(256, W::kMinBlocks) pool_kernel(const __grid_constant__ LaunchParams lp) {
   constexpr bool kOne = R::kOneJob;
+  static_assert(!(kOne && kTab), "a one-job launch has no job table");
   W s;
   R rng;
   if constexpr (kOne) rng.rk = lp.rk;
-  const JobDev *J = kOne ? &lp.job0 : lp.jobs;
+  const JobDev *jobs = lp.jobs;
+  const int64_t *job_begin = lp.job_begin;
+  if constexpr (kTab) {
+    JobDev *tab = reinterpret_cast<JobDev *>(vmc_smem);
+    int64_t *tbeg = reinterpret_cast<int64_t *>(vmc_smem + sizeof(JobDev) * (size_t)lp.njobs);
+    const int nw = lp.njobs * (int)(sizeof(JobDev) / sizeof(uint64_t));
+    const uint64_t *src = reinterpret_cast<const uint64_t *>(lp.jobs);
+    uint64_t *dst = reinterpret_cast<uint64_t *>(tab);
+    for (int i = threadIdx.x; i < nw; i += blockDim.x) dst[i] = __ldg(src + i);
+    for (int i = threadIdx.x; i <= lp.njobs; i += blockDim.x) tbeg[i] = __ldg(lp.job_begin + i);
+    __syncthreads();
+    jobs = tab;
+    job_begin = tbeg;
+  }
+  const JobDev *J = kOne ? &lp.job0 : jobs;
   Stage stg{nullptr, nullptr, 0u};
   if constexpr (W::kStaged) {
     if (lp.stage_slots > 0) {
@@ -91,7 +111,7 @@ __global__ void __launch_bounds__(256, W::kMinBlocks) pool_kernel(const __grid_c
       const int rank = __popc(need & lt_mask);
       if (((need >> lane) & 1u) && rank < avail) {
         const long long p = chunk_next + rank;
-        if constexpr (!kOne) J = lp.jobs + (lp.njobs > 1 ? find_job(lp, p) : 0);
+        if constexpr (!kOne) J = jobs + (lp.njobs > 1 ? find_job(job_begin, lp.njobs, p) : 0);
         const long long q = p - J->pbegin;
         start_rng(rng, *J, q);
         s.launch(*J, rng, q);

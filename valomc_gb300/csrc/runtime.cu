@@ -249,14 +249,15 @@ JobDev describe_job(const HostJob &j, const DeviceMesh &m, int precision, const 
   return d;
 }
 
-const void *select_kernel(const LaunchSpec &s, bool one) {
+const void *select_kernel(const LaunchSpec &s, bool one, bool tab) {
   // The one-job form is used for the FP32 walks only: for the FP64 walks it measured 2.3x
   // slower per element step than the per-job form on the 648k-tet phantom (same
   // trajectories, same registers), so they keep the descriptor and keys in global memory.
   one = one && !s.tape && s.precision == VMC_FP32;
+  tab = tab && !one;
   if (s.dim == 3)
-    return s.precision == VMC_FP64 ? kernel_3d64(s.fd, s.tape, one) : kernel_3d32(s.fd, s.tape, one);
-  return s.precision == VMC_FP64 ? kernel_2d64(s.fd, s.tape, one) : kernel_2d32(s.fd, s.tape, one);
+    return s.precision == VMC_FP64 ? kernel_3d64(s.fd, s.tape, one, tab) : kernel_3d32(s.fd, s.tape, one, tab);
+  return s.precision == VMC_FP64 ? kernel_2d64(s.fd, s.tape, one, tab) : kernel_2d32(s.fd, s.tape, one, tab);
 }
 
 void set_single_job(LaunchParams &lp, const JobDev &job) {
@@ -338,7 +339,7 @@ namespace {
 // its photon prefix.
 struct LaunchPlan {
   const void *fn = nullptr;
-  bool one = false;
+  bool one = false, tab = false;
   int grid = 0, block = 0, stage_slots = 0, dense = 0;
   size_t smem = 0;
   int64_t total = 0;
@@ -350,9 +351,11 @@ int plan_launch(int device, const LaunchSpec &spec, const std::vector<JobDev> &j
                 LaunchResult &res) {
   int sms = 0;
   VMC_TRY(select_device(device, &sms));
-  // the one-job kernels: FP32 walks on Philox streams (descriptor and keys as parameters)
+  // the one-job kernels: FP32 walks on Philox streams (descriptor and keys as parameters);
+  // the others copy a job table of up to kSmemJobs entries into each CTA's shared memory
   p.one = jobs_in.size() == 1 && !spec.tape && spec.precision == VMC_FP32;
-  p.fn = select_kernel(spec, p.one);
+  p.tab = !p.one && jobs_in.size() <= (size_t)kSmemJobs;
+  p.fn = select_kernel(spec, p.one, p.tab);
   if (!p.fn) { set_error("no kernel for this configuration"); return VMC_ERR_INVALID_ARGUMENT; }
   p.jobs = jobs_in;
   p.begin.assign(p.jobs.size() + 1, 0);
@@ -372,6 +375,7 @@ int plan_launch(int device, const LaunchSpec &spec, const std::vector<JobDev> &j
     while (p.stage_slots < spec.stage_slots && p.stage_slots < 4096) p.stage_slots <<= 1;
   }
   p.smem = (size_t)p.stage_slots * (sizeof(double) + sizeof(int32_t));
+  if (p.tab) p.smem = p.jobs.size() * sizeof(JobDev) + (p.jobs.size() + 1) * sizeof(int64_t);
   VMC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, p.fn, p.block, p.smem));
   if (per_sm < 1) { set_error("kernel does not fit on an SM at this block size"); return VMC_ERR_INVALID_ARGUMENT; }
   // A one-job launch on a small mesh, without the hashed stage: every CTA keeps the whole

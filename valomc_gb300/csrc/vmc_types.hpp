@@ -97,6 +97,8 @@ constexpr int kSlots = 64;
 constexpr int kDefaultRefill = 4;
 // largest accumulator set (2 Ne + 4 Nb doubles) a launch stages whole in each CTA's shared memory
 constexpr int64_t kDenseStageBytes = 32 * 1024;
+// largest job table a multi-job launch copies into each CTA's shared memory
+constexpr int kSmemJobs = 64;
 
 struct JobDev {
   const void *geom;            // Tet64 / Tet32 / Tri64 / Tri32 [Ne]
@@ -129,6 +131,7 @@ struct JobDev {
   unsigned long long *jc;      // [kSlots x kJcN]
   double *ledger;              // [kSlots x kLgN]
 };
+static_assert(sizeof(JobDev) % sizeof(uint64_t) == 0, "JobDev is copied as 8-byte words");
 
 // Launch-wide control block in device memory.
 struct Ctl {
