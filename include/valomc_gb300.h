@@ -220,13 +220,21 @@ int vmc_run_batch(vmc_mesh *const *meshes, const vmc_input *jobs, int32_t njobs,
                   const vmc_options *opt, vmc_output *outs, vmc_stats *stats, vmc_stats *job_stats);
 
 /* Autotuner: times short runs of a problem over block sizes x blocks per SM x fetch
- * chunks and writes the fastest into opt (precision and rng are kept). */
+ * chunks, then, on the fastest shape, the idle lanes a warp waits for before relaunching
+ * them (refill_lanes), and writes the result into opt (precision and rng are kept). */
 int vmc_autotune(vmc_mesh *const *meshes, const vmc_input *jobs, int32_t njobs, vmc_options *opt,
                  double budget_s);
 
 /* Serving: resident meshes, requests admitted by device-memory footprint, continuous
  * batching of request slots into short persistent launches. */
 typedef struct vmc_server vmc_server;
+enum vmc_slicing {
+  VMC_SLICE_DEFAULT = 0,         /* the server's choice: shortest remaining first */
+  VMC_SLICE_EQUAL = 1,           /* water-filling: requests below an equal share get all they
+                                    have left, the others share the rest equally */
+  VMC_SLICE_SHORTEST_FIRST = 2   /* every open request a floor of 1/4 of an equal share, the
+                                    rest to the requests with the fewest photons left first */
+};
 typedef struct vmc_server_config {
   int32_t device;
   int32_t precision;
@@ -238,6 +246,8 @@ typedef struct vmc_server_config {
                                  work at the measured rate while the backlog is small, up to
                                  the backlog and 0.5 s of work as it grows */
   int32_t block_size, blocks_per_sm;
+  int32_t slicing;            /* enum vmc_slicing: how an epoch's photons are shared among requests */
+  int32_t reserved;
 } vmc_server_config;
 int vmc_server_create(const vmc_server_config *cfg, vmc_server **out);
 int vmc_server_add_mesh(vmc_server *s, vmc_mesh *mesh, int32_t *mesh_id);   /* server borrows mesh */

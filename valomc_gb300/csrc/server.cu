@@ -176,11 +176,31 @@ void vmc_server::loop() {
     std::vector<Request *> open;
     for (Request *r : batch)
       if (r->status == VMC_OK && r->issued < r->nphoton) open.push_back(r);
-    // Slices by water-filling: a request with fewer photons left than an equal share of
-    // what remains gets all of them, and the others split the rest equally, so the epoch is
-    // as full as the open requests allow (equal shares left the small requests' unused
-    // share idle: underfilled epochs, a lower measured rate and smaller epochs after them).
-    {
+    // Slices.  Shortest remaining first (the default): every open request gets a floor of a
+    // quarter of an equal share, so none starves, and the rest of the epoch goes to the
+    // requests with the fewest photons left, in that order, so small and medium requests
+    // finish within one epoch instead of sharing it equally with the largest.
+    // Water-filling: a request with fewer photons left than an equal share of what remains
+    // gets all of them, and the others split the rest equally.  Both fill the epoch as far as
+    // the open requests allow (equal shares left the small requests' unused share idle:
+    // underfilled epochs, a lower measured rate and smaller epochs after them).
+    if (cfg.slicing != VMC_SLICE_EQUAL && !open.empty()) {
+      std::vector<Request *> by_left(open);
+      std::sort(by_left.begin(), by_left.end(),
+                [](const Request *a, const Request *b) { return a->nphoton - a->issued < b->nphoton - b->issued; });
+      const int64_t floor_share = std::max<int64_t>(1, epoch / (4 * (int64_t)by_left.size()));
+      int64_t left = epoch;
+      for (Request *r : by_left) {
+        r->slice = std::min(floor_share, r->nphoton - r->issued);
+        left -= r->slice;
+      }
+      for (Request *r : by_left) {
+        if (left <= 0) break;
+        const int64_t extra = std::min(left, r->nphoton - r->issued - r->slice);
+        r->slice += extra;
+        left -= extra;
+      }
+    } else {
       std::vector<Request *> by_left(open);
       std::sort(by_left.begin(), by_left.end(),
                 [](const Request *a, const Request *b) { return a->nphoton - a->issued < b->nphoton - b->issued; });
@@ -348,6 +368,7 @@ extern "C" {
 int vmc_server_create(const vmc_server_config *cfg, vmc_server **out) {
   if (!cfg || !out || cfg->max_slots <= 0 || cfg->memory_budget <= 0) return VMC_ERR_INVALID_ARGUMENT;
   if (cfg->precision != VMC_FP32 && cfg->precision != VMC_FP64) return VMC_ERR_INVALID_ARGUMENT;
+  if (cfg->slicing < VMC_SLICE_DEFAULT || cfg->slicing > VMC_SLICE_SHORTEST_FIRST) return VMC_ERR_INVALID_ARGUMENT;
   int s = select_device(cfg->device);
   if (s) return s;
   vmc_server *sv = new vmc_server;
