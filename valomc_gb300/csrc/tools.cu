@@ -219,7 +219,7 @@ int vmc_autotune(vmc_mesh *const *meshes, const vmc_input *jobs, int32_t njobs, 
         if (b == 256 && c == 32 && !half) dflt = rate;
         if (rate > best) { best = rate; bsp = sp; }
       }
-  if (dflt > 0 && best < 1.02 * dflt) {
+  if (dflt > 0 && best < 1.04 * dflt) {
     bsp = base;
     bsp.block = 256;
     bsp.chunk = 32;
@@ -228,7 +228,7 @@ int vmc_autotune(vmc_mesh *const *meshes, const vmc_input *jobs, int32_t njobs, 
   }
   // second stage, on the chosen shape: the idle lanes a warp waits for before relaunching
   // them (short walks gain from launching several photons together), kept at the default
-  // unless another count is 2% faster
+  // unless another count is 4% faster
   const double at_default = best;
   int best_refill = 0;
   for (int rf : refills) {
@@ -237,7 +237,7 @@ int vmc_autotune(vmc_mesh *const *meshes, const vmc_input *jobs, int32_t njobs, 
     double rate = 0;
     s = run(sp, frac, rate);
     if (s) return s;
-    if (rate > 1.02 * at_default && rate > best) { best = rate; best_refill = rf; }
+    if (rate > 1.04 * at_default && rate > best) { best = rate; best_refill = rf; }
   }
   opt->block_size = bsp.block;
   opt->fetch_chunk = bsp.chunk;
