@@ -352,9 +352,13 @@ int plan_launch(int device, const LaunchSpec &spec, const std::vector<JobDev> &j
   int sms = 0;
   VMC_TRY(select_device(device, &sms));
   // the one-job kernels: FP32 walks on Philox streams (descriptor and keys as parameters);
-  // the others copy a job table of up to kSmemJobs entries into each CTA's shared memory
+  // the others copy a job table of up to kSmemJobs entries into each CTA's shared memory,
+  // unless the launch stages deposits in a hashed shared-memory table (a single job on the
+  // replay tape), which starts at the same place
   p.one = jobs_in.size() == 1 && !spec.tape && spec.precision == VMC_FP32;
-  p.tab = !p.one && jobs_in.size() <= (size_t)kSmemJobs;
+  const bool staged = spec.stage_slots > 0 && spec.dim == 3 && spec.precision == VMC_FP32 && !spec.fd &&
+                      jobs_in.size() == 1;
+  p.tab = !p.one && !staged && jobs_in.size() <= (size_t)kSmemJobs;
   p.fn = select_kernel(spec, p.one, p.tab);
   if (!p.fn) { set_error("no kernel for this configuration"); return VMC_ERR_INVALID_ARGUMENT; }
   p.jobs = jobs_in;
@@ -370,7 +374,7 @@ int plan_launch(int device, const LaunchSpec &spec, const std::vector<JobDev> &j
   int per_sm = 0;
   // shared-memory staging of deposits: FP32 tetrahedral walk, continuous wave, one job
   p.stage_slots = 0;
-  if (spec.stage_slots > 0 && spec.dim == 3 && spec.precision == VMC_FP32 && !spec.fd && p.jobs.size() == 1) {
+  if (staged) {
     p.stage_slots = 1;
     while (p.stage_slots < spec.stage_slots && p.stage_slots < 4096) p.stage_slots <<= 1;
   }
