@@ -466,6 +466,8 @@ def run_serve(args, dev=0):
     out = {"workload": "8 cubes 50k-2M tets, cosinic disk / gaussian sources, photons logU[1e5,1e7]",
            "rate_hz": args.serve_rate, "window_s": T, "requests": len(sub), "slicing": args.serve_slicing,
            "submit_s": t_sub, "drain_s": wall - t_sub,
+           # the mix's mean request is 1e5..1e7 log-uniform: (1e7 - 1e5) / ln(100) photons
+           "offered_expected_photons_per_s": args.serve_rate * (1e7 - 1e5) / math.log(100.0),
            "offered_photons_per_s": offered, "served_photons_per_s_incl_drain": ph / wall,
            "offered_photons_per_s_steady": offered_steady, "served_photons_per_s_steady": served_steady,
            "served_steps_per_s": steps / wall, "steps_per_photon": steps / max(ph, 1),
