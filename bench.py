@@ -419,16 +419,19 @@ def run_serve(args, dev=0):
     from valomc_gb300 import meshgen as mg
     mix = mg.ServingMix(seed=5)
     meshes = [V.Mesh(b, device=dev) for b in mix.base]
+    if args.serve_seed:  # another sample of the same stream: same meshes, other requests and arrivals
+        mix.rng = np.random.default_rng(1000 + args.serve_seed)
 
     def server():
         srv = V.Server(max_slots=args.serve_slots, memory_budget=16 << 30, epoch_photons=int(args.serve_epoch),
-                       block_size=args.serve_block, device=dev, slicing=args.serve_slicing)
+                       block_size=args.serve_block, device=dev, slicing=args.serve_slicing,
+                       epoch_max_ms=args.serve_epoch_max_ms)
         return srv, [srv.add_mesh(m) for m in meshes]
 
     srv, ids = server()
     k, p = mix.request()
     srv.wait(srv.submit(ids[k], p.copy(Nphoton=10000)))  # warm the kernels and graphs
-    rng = np.random.default_rng(55)
+    rng = np.random.default_rng(55 + args.serve_seed)
     T = args.serve_window
     t0 = time.time()
     t, sub = 0.0, []
@@ -465,6 +468,7 @@ def run_serve(args, dev=0):
     q2, q4 = float(np.median(lat[q:2 * q])), float(np.median(lat[-q:]))
     out = {"workload": "8 cubes 50k-2M tets, cosinic disk / gaussian sources, photons logU[1e5,1e7]",
            "rate_hz": args.serve_rate, "window_s": T, "requests": len(sub), "slicing": args.serve_slicing,
+           "epoch_max_ms": args.serve_epoch_max_ms, "sample": args.serve_seed,
            "submit_s": t_sub, "drain_s": wall - t_sub,
            # the mix's mean request is 1e5..1e7 log-uniform: (1e7 - 1e5) / ln(100) photons
            "offered_expected_photons_per_s": args.serve_rate * (1e7 - 1e5) / math.log(100.0),
@@ -522,6 +526,10 @@ def main():
     ap.add_argument("--serve-block", type=int, default=0, help="threads per CTA of the serving launches (0: default)")
     ap.add_argument("--serve-slicing", type=int, default=0,
                     help="serving slices: 0 the server's default, 1 water-filling, 2 shortest remaining first")
+    ap.add_argument("--serve-seed", type=int, default=0,
+                    help="0: the default sample of requests and arrivals; k > 0: another sample")
+    ap.add_argument("--serve-epoch-max-ms", type=int, default=0,
+                    help="cap of the serving loop's epochs, ms of work (0: the server's default)")
     ap.add_argument("--serve-capacity", type=int, default=1, help="1: also time the same requests submitted at once")
     args = ap.parse_args()
     if args.impl == "reference":

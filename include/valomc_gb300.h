@@ -244,10 +244,13 @@ typedef struct vmc_server_config {
                                  to the device's free memory (less 256 MiB) at creation */
   int64_t epoch_photons;      /* photons per launch across all slots; 0 = by load: 50 ms of
                                  work at the measured rate while the backlog is small, up to
-                                 the backlog and 0.5 s of work as it grows */
+                                 the backlog and epoch_max_ms of work as it grows */
   int32_t block_size, blocks_per_sm;
   int32_t slicing;            /* enum vmc_slicing: how an epoch's photons are shared among requests */
-  int32_t reserved;
+  int32_t epoch_max_ms;       /* cap of an epoch sized by load, in ms of work at the measured
+                                 rate (>= 50); 0 = 500.  Larger epochs pay the end-of-launch
+                                 drain less often (capacity); smaller ones let new requests
+                                 in sooner (latency) */
 } vmc_server_config;
 int vmc_server_create(const vmc_server_config *cfg, vmc_server **out);
 int vmc_server_add_mesh(vmc_server *s, vmc_mesh *mesh, int32_t *mesh_id);   /* server borrows mesh */

@@ -107,3 +107,14 @@ def test_python_structs_have_the_headers_layout(built):
         assert c[(cname, "sizeof")] == ctypes.sizeof(py), cname
         for f in py._fields_:
             assert c[(cname, f[0])] == getattr(py, f[0]).offset, (cname, f[0])
+
+
+@pytest.mark.parametrize("bad", [dict(slicing=3), dict(slicing=-1), dict(epoch_max_ms=-5), dict(epoch_max_ms=20),
+                                 dict(max_slots=0), dict(memory_budget=0), dict(precision=7)])
+def test_server_config_is_checked_before_any_device_work(built, bad):
+    """vmc_server_create refuses an invalid configuration with VMC_ERR_INVALID_ARGUMENT
+    before it selects a device, so these run without a GPU."""
+    from valomc_gb300 import api
+    with pytest.raises(api.VmcError) as e:
+        api.Server(**bad)
+    assert api.STATUS[e.value.status] == "VMC_ERR_INVALID_ARGUMENT"

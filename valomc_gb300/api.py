@@ -98,7 +98,7 @@ class VmcServerConfig(C.Structure):
     _fields_ = [
         ("device", C.c_int32), ("precision", C.c_int32), ("max_slots", C.c_int32), ("use_graph", C.c_int32),
         ("memory_budget", C.c_int64), ("epoch_photons", C.c_int64), ("block_size", C.c_int32),
-        ("blocks_per_sm", C.c_int32), ("slicing", C.c_int32), ("reserved", C.c_int32),
+        ("blocks_per_sm", C.c_int32), ("slicing", C.c_int32), ("epoch_max_ms", C.c_int32),
     ]
 
 
@@ -384,9 +384,9 @@ class Server:
     continuous batching of admitted requests."""
 
     def __init__(self, precision=VMC_FP32, max_slots=32, memory_budget=8 << 30, epoch_photons=0, device=0,
-                 block_size=0, blocks_per_sm=0, use_graph=True, slicing=0):
+                 block_size=0, blocks_per_sm=0, use_graph=True, slicing=0, epoch_max_ms=0):
         cfg = VmcServerConfig(device, precision, max_slots, int(bool(use_graph)), memory_budget, epoch_photons,
-                              block_size, blocks_per_sm, slicing, 0)
+                              block_size, blocks_per_sm, slicing, epoch_max_ms)
         h = C.c_void_p()
         s = lib().vmc_server_create(C.byref(cfg), C.byref(h))
         if s:

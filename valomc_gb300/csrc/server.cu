@@ -1,6 +1,7 @@
 // server.cu -- serving loop: resident meshes, requests admitted into slots by their
 // device-memory footprint, continuous batching of all admitted requests into persistent
-// launches ("epochs") sized by the backlog (50 ms of work when it is small, up to 0.5 s).
+// launches ("epochs") sized by the backlog (50 ms of work when it is small, up to a cap,
+// 0.5 s by default).
 //
 // Epochs alternate between two streams ("lanes"): the next epoch is queued while the
 // current one runs, so it takes the SMs as the running launch drains.
@@ -164,13 +165,15 @@ void vmc_server::loop() {
     if (!admitted.empty()) cudaStreamSynchronize(L.st);
     // epoch: a slice of every active request with photons left, one launch per class.  Its
     // size follows the load: 50 ms of work while the backlog is small (latency), up to the
-    // backlog and at most 0.5 s of work as it grows.  Every launch ends in a drain (CTAs
-    // keep their SM slot until their slowest walk ends); larger epochs pay it less often,
-    // so the loop's capacity rises with the load that needs it.
+    // backlog and at most epoch_max_ms (0.5 s) of work as it grows.  Every launch ends in a
+    // drain (CTAs keep their SM slot until their slowest walk ends); larger epochs pay it
+    // less often, so the loop's capacity rises with the load that needs it, while a request
+    // that arrives waits for up to two epochs (the running one and the one queued).
     int64_t epoch = cfg.epoch_photons;
     if (epoch <= 0) {
+      const double max_s = (cfg.epoch_max_ms > 0 ? cfg.epoch_max_ms : 500) * 1e-3;
       const int64_t lo = std::max<int64_t>(200000, (int64_t)(rate * 0.05));
-      const int64_t hi = std::max<int64_t>(lo, (int64_t)(rate * 0.5));
+      const int64_t hi = std::max<int64_t>(lo, (int64_t)(rate * max_s));
       epoch = std::min(hi, std::max(lo, backlog));
     }
     std::vector<Request *> open;
@@ -369,6 +372,7 @@ int vmc_server_create(const vmc_server_config *cfg, vmc_server **out) {
   if (!cfg || !out || cfg->max_slots <= 0 || cfg->memory_budget <= 0) return VMC_ERR_INVALID_ARGUMENT;
   if (cfg->precision != VMC_FP32 && cfg->precision != VMC_FP64) return VMC_ERR_INVALID_ARGUMENT;
   if (cfg->slicing < VMC_SLICE_DEFAULT || cfg->slicing > VMC_SLICE_SHORTEST_FIRST) return VMC_ERR_INVALID_ARGUMENT;
+  if (cfg->epoch_max_ms < 0 || (cfg->epoch_max_ms > 0 && cfg->epoch_max_ms < 50)) return VMC_ERR_INVALID_ARGUMENT;
   int s = select_device(cfg->device);
   if (s) return s;
   vmc_server *sv = new vmc_server;

@@ -411,20 +411,23 @@ struct Walk2D32 {
     const float4 *L4 = reinterpret_cast<const float4 *>(T->ln);
     const float4 l0 = __ldg(L4 + 0), l1 = __ldg(L4 + 1), l2 = __ldg(L4 + 2);
     const int4 nb = __ldg(reinterpret_cast<const int4 *>(T->nbr));
-    float best = INFINITY;
+    // selects over all three edges, no branch per edge; num / nd compared by cross
+    // products, one reciprocal for the winning edge (bnd = 0: none yet)
+    float bnum = 1.0f, bnd = 0.0f;
     int nf = -1;
     {
       const float4 ln[3] = {l0, l1, l2};
 #pragma unroll
-      for (int f = 0; f < 3; f++) {  // selects over all three edges, no branch per edge
+      for (int f = 0; f < 3; f++) {
         const float nd = ln[f].x * dx + ln[f].y * dy;
         const float num = ln[f].z - (ln[f].x * px + ln[f].y * py);
-        const float t = nd > 0.0f ? __fdividef(num, nd) : INFINITY;
-        const bool better = t < best;
-        best = better ? t : best;
+        const bool better = nd > 0.0f && num * bnd < bnum * nd;
+        bnum = better ? num : bnum;
+        bnd = better ? nd : bnd;
         nf = better ? f : nf;
       }
     }
+    const float best = __fdividef(bnum, bnd);
     if (nf < 0) {
       job_count(J, kJcLoss); job_ledger(J, kLgLost, f2d_int(w));
       die(J, kEvLost);

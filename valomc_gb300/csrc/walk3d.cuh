@@ -556,8 +556,11 @@ struct Walk3D32 {
     const float4 p0 = __ldg(P4 + 0), p1 = __ldg(P4 + 1), p2 = __ldg(P4 + 2), p3 = __ldg(P4 + 3);
     const int4 nb = __ldg(reinterpret_cast<const int4 *>(T->nbr));
     // exit: nearest face the direction points out of, as selects over all four faces (no
-    // branch per face: fewer divergent regions and 6 fewer registers)
-    float best = INFINITY;
+    // branch per face: fewer divergent regions and 6 fewer registers).  The distances
+    // num / nd (nd > 0) are compared as num_f bnd < bnum nd_f, so that only the winning
+    // face's quotient is computed: one reciprocal per step instead of four (bnd = 0 stands
+    // for "none yet")
+    float bnum = 1.0f, bnd = 0.0f;
     int nf = -1;
     {
       const float4 pl[4] = {p0, p1, p2, p3};
@@ -565,12 +568,13 @@ struct Walk3D32 {
       for (int f = 0; f < 4; f++) {
         const float nd = pl[f].x * dx + pl[f].y * dy + pl[f].z * dz;
         const float num = pl[f].w - (pl[f].x * px + pl[f].y * py + pl[f].z * pz);
-        const float t = nd > 0.0f ? __fdividef(num, nd) : INFINITY;
-        const bool better = t < best;
-        best = better ? t : best;
+        const bool better = nd > 0.0f && num * bnd < bnum * nd;
+        bnum = better ? num : bnum;
+        bnd = better ? nd : bnd;
         nf = better ? f : nf;
       }
     }
+    const float best = __fdividef(bnum, bnd);
     if (nf < 0) {
       job_count(J, kJcLoss); job_ledger(J, kLgLost, f2d_int(w));
       die(J, kEvLost);
