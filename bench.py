@@ -414,13 +414,16 @@ def run_serve(args, dev=0):
     """Poisson request stream at --serve-rate over 8 resident cubes (50k-2M tets),
     cosinic-disk or Gaussian sources at random top points, config-4 optics, photons
     log-uniform 1e5-1e7, for --serve-window seconds; then the same requests submitted at
-    once (the loop's capacity for this mix)."""
+    once (the loop's capacity for this mix).  --serve-samples > 1 adds further samples of
+    the same stream (other requests and arrival times on the same meshes), summarised in
+    `other_samples`: one 10 s sample's offered load varies by several percent around the
+    stream's mean."""
+    import copy
     import valomc_gb300 as V
     from valomc_gb300 import meshgen as mg
     mix = mg.ServingMix(seed=5)
     meshes = [V.Mesh(b, device=dev) for b in mix.base]
-    if args.serve_seed:  # another sample of the same stream: same meshes, other requests and arrivals
-        mix.rng = np.random.default_rng(1000 + args.serve_seed)
+    rng0 = copy.deepcopy(mix.rng)
 
     def server():
         srv = V.Server(max_slots=args.serve_slots, memory_budget=16 << 30, epoch_photons=int(args.serve_epoch),
@@ -428,61 +431,67 @@ def run_serve(args, dev=0):
                        epoch_max_ms=args.serve_epoch_max_ms)
         return srv, [srv.add_mesh(m) for m in meshes]
 
-    srv, ids = server()
-    k, p = mix.request()
-    srv.wait(srv.submit(ids[k], p.copy(Nphoton=10000)))  # warm the kernels and graphs
-    rng = np.random.default_rng(55 + args.serve_seed)
-    T = args.serve_window
-    t0 = time.time()
-    t, sub = 0.0, []
-    while True:
-        t += rng.exponential(1.0 / args.serve_rate)
-        if t > T:
-            break
+    def sample(seed):
+        # seed 0: the default sample; k > 0: the same meshes, other requests and arrivals
+        mix.rng = copy.deepcopy(rng0) if seed == 0 else np.random.default_rng(1000 + seed)
+        srv, ids = server()
         k, p = mix.request()
-        now = time.time() - t0
-        if t > now:
-            time.sleep(t - now)
-        sub.append((srv.submit(ids[k], p), p.Nphoton, time.time() - t0, k, p))
-    t_sub = time.time() - t0
-    lat, fin, ph, steps = [], [], 0, 0
-    for rid, n, ts, _, _ in sub:
-        r = srv.wait(rid)
-        lat.append(r.stats["seconds_total"])
-        fin.append(ts + r.stats["seconds_total"])
-        ph += n
-        steps += r.stats["steps"]
-    wall = time.time() - t0
-    srv.close()
-    n_sub = np.array([x[1] for x in sub], float)
-    t_in = np.array([x[2] for x in sub])
-    fin = np.array(fin)
-    lat = np.array(lat)
-    offered = n_sub.sum() / T
-    # steady state: the last three quarters of the window (the first is the start-up from
-    # an empty device); the photons of requests that finished in it, against those offered
-    lo = T / 4
-    served_steady = n_sub[(fin >= lo) & (fin <= T)].sum() / (T - lo)
-    offered_steady = n_sub[(t_in >= lo) & (t_in <= T)].sum() / (T - lo)
-    q = max(1, len(lat) // 4)
-    q2, q4 = float(np.median(lat[q:2 * q])), float(np.median(lat[-q:]))
+        srv.wait(srv.submit(ids[k], p.copy(Nphoton=10000)))  # warm the kernels and graphs
+        rng = np.random.default_rng(55 + seed)
+        T = args.serve_window
+        t0 = time.time()
+        t, sub = 0.0, []
+        while True:
+            t += rng.exponential(1.0 / args.serve_rate)
+            if t > T:
+                break
+            k, p = mix.request()
+            now = time.time() - t0
+            if t > now:
+                time.sleep(t - now)
+            sub.append((srv.submit(ids[k], p), p.Nphoton, time.time() - t0, k, p))
+        t_sub = time.time() - t0
+        lat, fin, ph, steps = [], [], 0, 0
+        for rid, n, ts, _, _ in sub:
+            r = srv.wait(rid)
+            lat.append(r.stats["seconds_total"])
+            fin.append(ts + r.stats["seconds_total"])
+            ph += n
+            steps += r.stats["steps"]
+        wall = time.time() - t0
+        srv.close()
+        n_sub = np.array([x[1] for x in sub], float)
+        t_in = np.array([x[2] for x in sub])
+        fin = np.array(fin)
+        lat = np.array(lat)
+        offered = n_sub.sum() / T
+        # steady state: the last three quarters of the window (the first is the start-up from
+        # an empty device); the photons of requests that finished in it, against those offered
+        lo = T / 4
+        served_steady = n_sub[(fin >= lo) & (fin <= T)].sum() / (T - lo)
+        offered_steady = n_sub[(t_in >= lo) & (t_in <= T)].sum() / (T - lo)
+        q = max(1, len(lat) // 4)
+        q2, q4 = float(np.median(lat[q:2 * q])), float(np.median(lat[-q:]))
+        out = {"sample": seed, "requests": len(sub), "submit_s": t_sub, "drain_s": wall - t_sub,
+               "offered_photons_per_s": offered, "served_photons_per_s_incl_drain": ph / wall,
+               "offered_photons_per_s_steady": offered_steady, "served_photons_per_s_steady": served_steady,
+               "served_steps_per_s": steps / wall, "steps_per_photon": steps / max(ph, 1),
+               # stable: in the steady part of the window the device serves >= 95% of what is
+               # offered, and the latency does not grow (median of the last quarter of requests
+               # at most twice the second quarter's, plus 50 ms)
+               "stable": bool(served_steady >= 0.95 * offered_steady and q4 <= 2.0 * q2 + 0.05),
+               "p50_second_quarter_s": q2, "p50_last_quarter_s": q4,
+               "p50_s": float(np.percentile(lat, 50)), "p90_s": float(np.percentile(lat, 90)),
+               "p99_s": float(np.percentile(lat, 99)),
+               "p50_small_s": float(np.median(lat[n_sub < 1e6])) if (n_sub < 1e6).any() else None}
+        return out, sub, n_sub
+
+    out, sub, n_sub = sample(args.serve_seed)
     out = {"workload": "8 cubes 50k-2M tets, cosinic disk / gaussian sources, photons logU[1e5,1e7]",
-           "rate_hz": args.serve_rate, "window_s": T, "requests": len(sub), "slicing": args.serve_slicing,
-           "epoch_max_ms": args.serve_epoch_max_ms, "sample": args.serve_seed,
-           "submit_s": t_sub, "drain_s": wall - t_sub,
+           "rate_hz": args.serve_rate, "window_s": args.serve_window, "slicing": args.serve_slicing,
+           "epoch_max_ms": args.serve_epoch_max_ms,
            # the mix's mean request is 1e5..1e7 log-uniform: (1e7 - 1e5) / ln(100) photons
-           "offered_expected_photons_per_s": args.serve_rate * (1e7 - 1e5) / math.log(100.0),
-           "offered_photons_per_s": offered, "served_photons_per_s_incl_drain": ph / wall,
-           "offered_photons_per_s_steady": offered_steady, "served_photons_per_s_steady": served_steady,
-           "served_steps_per_s": steps / wall, "steps_per_photon": steps / max(ph, 1),
-           # stable: in the steady part of the window the device serves >= 95% of what is
-           # offered, and the latency does not grow (median of the last quarter of requests
-           # at most twice the second quarter's, plus 50 ms)
-           "stable": bool(served_steady >= 0.95 * offered_steady and q4 <= 2.0 * q2 + 0.05),
-           "p50_second_quarter_s": q2, "p50_last_quarter_s": q4,
-           "p50_s": float(np.percentile(lat, 50)), "p90_s": float(np.percentile(lat, 90)),
-           "p99_s": float(np.percentile(lat, 99)),
-           "p50_small_s": float(np.median(lat[n_sub < 1e6])) if (n_sub < 1e6).any() else None}
+           "offered_expected_photons_per_s": args.serve_rate * (1e7 - 1e5) / math.log(100.0), **out}
     if args.serve_capacity:
         srv, ids = server()
         srv.wait(srv.submit(ids[sub[0][3]], sub[0][4].copy(Nphoton=10000)))
@@ -492,6 +501,14 @@ def run_serve(args, dev=0):
             srv.wait(r)
         out["capacity_photons_per_s"] = n_sub.sum() / (time.time() - t0)
         srv.close()
+    keys = ("sample", "offered_photons_per_s", "offered_photons_per_s_steady", "served_photons_per_s_steady",
+            "stable", "p50_second_quarter_s", "p50_last_quarter_s", "p50_s", "p99_s")
+    others = []
+    for k in range(1, args.serve_samples):
+        o, _, _ = sample(args.serve_seed + k)
+        others.append({key: o[key] for key in keys})
+    if others:
+        out["other_samples"] = others
     for m in meshes:
         m.close()
     return out
@@ -526,6 +543,8 @@ def main():
     ap.add_argument("--serve-block", type=int, default=0, help="threads per CTA of the serving launches (0: default)")
     ap.add_argument("--serve-slicing", type=int, default=0,
                     help="serving slices: 0 the server's default, 1 water-filling, 2 shortest remaining first")
+    ap.add_argument("--serve-samples", type=int, default=2,
+                    help="samples of the request stream: the default one, then others on the same meshes")
     ap.add_argument("--serve-seed", type=int, default=0,
                     help="0: the default sample of requests and arrivals; k > 0: another sample")
     ap.add_argument("--serve-epoch-max-ms", type=int, default=0,
