@@ -122,5 +122,9 @@ const void *kernel_2d32(bool fd, bool tape, bool one, bool tab);
 // tab: the per-job form with the job table copied into each CTA's shared memory
 const void *select_kernel(const LaunchSpec &s, bool one = false, bool tab = false);
 void set_single_job(LaunchParams &lp, const JobDev &job);
+// the L1 / shared-memory split of a pool kernel: reset to the driver's default before the
+// occupancy query, then the smallest split holding per_sm CTAs' shared memory
+void reset_carveout(const void *fn);
+void fit_carveout(const void *fn, int device, int per_sm, size_t dyn_smem);
 
 }  // namespace vmc

@@ -235,9 +235,11 @@ extern "C" int vmc_run_noalloc(vmc_mesh *mesh, const vmc_input *job, const vmc_o
   const int block = o.block_size > 0 ? o.block_size : 256;
   if (block % 32 || block > 256) return VMC_ERR_INVALID_ARGUMENT;  // the pool kernels run <= 256 threads
   int per_sm = 0;
+  reset_carveout(fn);
   VMC_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, 0));
   if (o.blocks_per_sm > 0) per_sm = std::min(per_sm, (int)o.blocks_per_sm);
   if (per_sm < 1) return VMC_ERR_INVALID_ARGUMENT;
+  fit_carveout(fn, o.device, per_sm, 0);
   LaunchParams lp{};
   lp.jobs = reinterpret_cast<const JobDev *>(base + kOffJob);
   lp.job_begin = reinterpret_cast<const int64_t *>(base + kOffBegin);

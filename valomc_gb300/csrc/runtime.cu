@@ -260,6 +260,31 @@ const void *select_kernel(const LaunchSpec &s, bool one, bool tab) {
   return s.precision == VMC_FP64 ? kernel_2d64(s.fd, s.tape, one, tab) : kernel_2d32(s.fd, s.tape, one, tab);
 }
 
+// The SM's unified L1 / shared-memory array is split per launch.  Left to itself the driver
+// gave the pool kernels more shared memory than they use, at the cost of L1, where each
+// step's element record is re-read after a scatter; preferring the smallest split that
+// still holds every resident CTA's static and dynamic shared memory (plus the 1 KiB the
+// hardware reserves per CTA) was 2.3% faster on the 648k-tet phantom and 1.8% on the
+// serving mix, and changed nothing on meshes staged whole in shared memory.  The occupancy
+// is taken at the driver's default split (reset_carveout) and the split fitted after it.
+void reset_carveout(const void *fn) {
+  cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, -1);
+  cudaGetLastError();  // a hint: a refusal leaves the default split
+}
+
+void fit_carveout(const void *fn, int device, int per_sm, size_t dyn_smem) {
+  cudaFuncAttributes fa;
+  int smem_sm = 0;
+  if (cudaFuncGetAttributes(&fa, fn) == cudaSuccess &&
+      cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device) == cudaSuccess &&
+      smem_sm > 0) {
+    const double need = (double)per_sm * (double)(fa.sharedSizeBytes + dyn_smem + 1024);
+    const int pct = std::min(100, (int)std::ceil(100.0 * need / smem_sm) + 1);
+    cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+  }
+  cudaGetLastError();
+}
+
 void set_single_job(LaunchParams &lp, const JobDev &job) {
   lp.job0 = job;
   // Philox4x32-10 key schedule: round r uses key + r * (0x9E3779B9, 0xBB67AE85) mod 2^32
@@ -361,6 +386,7 @@ int plan_launch(int device, const LaunchSpec &spec, const std::vector<JobDev> &j
   p.tab = !p.one && !staged && jobs_in.size() <= (size_t)kSmemJobs;
   p.fn = select_kernel(spec, p.one, p.tab);
   if (!p.fn) { set_error("no kernel for this configuration"); return VMC_ERR_INVALID_ARGUMENT; }
+  reset_carveout(p.fn);
   p.jobs = jobs_in;
   p.begin.assign(p.jobs.size() + 1, 0);
   for (size_t i = 0; i < p.jobs.size(); i++) {
@@ -405,6 +431,7 @@ int plan_launch(int device, const LaunchSpec &spec, const std::vector<JobDev> &j
   }
   if (spec.blocks_per_sm > 0) per_sm = std::min(per_sm, spec.blocks_per_sm);
   p.grid = per_sm * sms;
+  fit_carveout(p.fn, device, per_sm, p.smem);
   res.grid = p.grid;
   res.block = p.block;
   return VMC_OK;

@@ -209,6 +209,7 @@ int vmc_autotune(vmc_mesh *const *meshes, const vmc_input *jobs, int32_t njobs, 
         sp.chunk = c;
         if (half) {
           int per_sm = 0;
+          reset_carveout(select_kernel(sp));  // occupancy at the default split, as the launch plans it
           cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, select_kernel(sp), b, 0);
           if (per_sm < 2) continue;
           sp.blocks_per_sm = per_sm / 2;

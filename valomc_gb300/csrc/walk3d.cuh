@@ -480,8 +480,12 @@ struct Walk3D32 {
     float ct;
     if (g != 0.0f) {
       if (xi > 0.0f && xi < 1.0f) {
-        float q = __fdividef(1.0f - g * g, 1.0f - g + 2.0f * g * xi);
-        ct = __fdividef(1.0f + g * g - q * q, 2.0f * g);
+        // (1 + g^2 - q^2) / (2 g) with q = (1 - g^2) / D, D = 1 - g + 2 g xi, over one
+        // division: ((1 + g^2) D^2 - (1 - g^2)^2) / (2 g D^2)
+        const float D = 1.0f - g + 2.0f * g * xi;
+        const float a = 1.0f - g * g;
+        const float D2 = D * D;
+        ct = __fdividef((1.0f + g * g) * D2 - a * a, 2.0f * g * D2);
       } else {
         ct = xi > 0.5f ? 1.0f : -1.0f;  // theta = (1 - xi) pi at xi in {0, 1}
       }
@@ -495,17 +499,18 @@ struct Walk3D32 {
     // phi uniform on [-pi, pi] (the reference's [0, 2 pi] shifted; same distribution)
     __sincosf((float)kPi * (2.0f * unif_closed_f(rng) - 1.0f), &sp, &cp);
     float nx, ny, nz;
-    if (fabsf(dz) > 0.999f) {
-      nx = st * cp;
-      ny = st * sp;
-      nz = dz > 0.0f ? ct : -ct;  // cos(theta) times the sign of dz (not |cos| with that sign)
-    } else {
-      const float s2z = 1.0f - dz * dz;
+    {
+      // the general rotation and the near-pole case (|dz| > 0.999) as selects, no branch
+      const bool pole = fabsf(dz) > 0.999f;
+      const float s2z = pole ? 1.0f : 1.0f - dz * dz;
       const float isq = rsqrtf(s2z);
       const float sq = s2z * isq;
-      nx = st * (dx * dz * cp - dy * sp) * isq + dx * ct;
-      ny = st * (dy * dz * cp + dx * sp) * isq + dy * ct;
-      nz = -st * cp * sq + dz * ct;
+      const float rx = st * (dx * dz * cp - dy * sp) * isq + dx * ct;
+      const float ry = st * (dy * dz * cp + dx * sp) * isq + dy * ct;
+      const float rz = -st * cp * sq + dz * ct;
+      nx = pole ? st * cp : rx;
+      ny = pole ? st * sp : ry;
+      nz = pole ? (dz > 0.0f ? ct : -ct) : rz;  // cos(theta) times the sign of dz (not |cos| with that sign)
     }
     float in = rsqrtf(nx * nx + ny * ny + nz * nz);
     dx = nx * in; dy = ny * in; dz = nz * in;
