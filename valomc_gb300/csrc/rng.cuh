@@ -16,8 +16,8 @@ namespace vmc {
 // shared-memory slot of the lane, read once per block, so that only the words that change
 // occupy registers.  A pool kernel runs at most 256 threads per CTA.  A one-job launch
 // takes its round keys from the kernel parameters, so its slot holds the photon's high
-// word and the stream only: 2 KB per CTA instead of 4, which lets the launch's L1 /
-// shared-memory split give L1 another 16 KB (+0.8% on the 648k-tet phantom).
+// word and the stream only: an 8-byte read per block instead of 16 (half the shared-memory
+// wavefronts) and 2 KB per CTA instead of 4 (+0.8% on the 648k-tet phantom).
 __device__ __forceinline__ uint4 *philox_slot() {
   __shared__ uint4 slots[256];
   return slots + threadIdx.x;
