@@ -28,6 +28,7 @@
 #include <vector>
 
 #include "engine.hpp"
+#include "epoch_plan.hpp"
 
 namespace vmc {
 DeviceMesh *mesh_impl(vmc_mesh *m);
@@ -159,7 +160,7 @@ void vmc_server::loop() {
   for (;;) {
     // Late binding: the next epoch is built when most of the running one's photons have
     // been handed out, not as soon as it starts, so that requests arriving meanwhile ride
-    // in it: a request waits for up to one epoch instead of two (at 50 req/s on the serving
+    // in it: a request waits for about one epoch instead of up to two (at 50 req/s on the serving
     // mix, median latency 0.14 s against 0.17 s, no change in capacity).
     if (probe && hnext) wait_until_drain_nears(*this, lanes[cur ^ 1], probe, hnext);
     std::vector<Request *> admitted;
@@ -216,60 +217,22 @@ void vmc_server::loop() {
     }
     if (!admitted.empty()) cudaStreamSynchronize(L.st);
     // epoch: a slice of every active request with photons left, one launch per class.  Its
-    // size follows the load: 50 ms of work while the backlog is small (latency), up to the
-    // backlog and at most epoch_max_ms (0.5 s) of work as it grows.  Every launch ends in a
-    // drain (CTAs keep their SM slot until their slowest walk ends); larger epochs pay it
-    // less often, so the loop's capacity rises with the load that needs it, while a request
-    // that arrives waits for up to two epochs (the running one and the one queued).
-    int64_t epoch = cfg.epoch_photons;
-    if (epoch <= 0) {
-      const double max_s = (cfg.epoch_max_ms > 0 ? cfg.epoch_max_ms : 500) * 1e-3;
-      const int64_t lo = std::max<int64_t>(200000, (int64_t)(rate * 0.05));
-      const int64_t hi = std::max<int64_t>(lo, (int64_t)(rate * max_s));
-      epoch = std::min(hi, std::max(lo, backlog));
-    }
+    // size follows the load (epoch_photons): 50 ms of work while the backlog is small
+    // (latency), up to the backlog and at most epoch_max_ms (0.5 s) of work as it grows.
+    // Every launch ends in a drain (CTAs keep their SM slot until their slowest walk ends);
+    // larger epochs pay it less often, so the loop's capacity rises with the load that needs
+    // it, while a request that arrives waits for about one epoch (late binding, above).
+    const int64_t epoch = epoch_photons(cfg.epoch_photons, rate, cfg.epoch_max_ms, backlog);
     std::vector<Request *> open;
     for (Request *r : batch)
       if (r->status == VMC_OK && r->issued < r->nphoton) open.push_back(r);
-    // Slices.  Shortest remaining first (the default): every open request gets a floor of a
-    // quarter of an equal share, so none starves, and the rest of the epoch goes to the
-    // requests with the fewest photons left, in that order, so small and medium requests
-    // finish within one epoch instead of sharing it equally with the largest.
-    // Water-filling: a request with fewer photons left than an equal share of what remains
-    // gets all of them, and the others split the rest equally.  Both fill the epoch as far as
-    // the open requests allow (equal shares left the small requests' unused share idle:
-    // underfilled epochs, a lower measured rate and smaller epochs after them).
-    if (cfg.slicing != VMC_SLICE_EQUAL && !open.empty()) {
-      std::vector<Request *> by_left(open);
-      std::sort(by_left.begin(), by_left.end(),
-                [](const Request *a, const Request *b) { return a->nphoton - a->issued < b->nphoton - b->issued; });
-      const int64_t floor_share = std::max<int64_t>(1, epoch / (4 * (int64_t)by_left.size()));
-      int64_t left = epoch;
-      for (Request *r : by_left) {
-        r->slice = std::min(floor_share, r->nphoton - r->issued);
-        left -= r->slice;
-      }
-      for (Request *r : by_left) {
-        if (left <= 0) break;
-        const int64_t extra = std::min(left, r->nphoton - r->issued - r->slice);
-        r->slice += extra;
-        left -= extra;
-      }
-    } else {
-      std::vector<Request *> by_left(open);
-      std::sort(by_left.begin(), by_left.end(),
-                [](const Request *a, const Request *b) { return a->nphoton - a->issued < b->nphoton - b->issued; });
-      int64_t left = epoch;
-      size_t k = 0;
-      for (; k < by_left.size(); k++) {
-        Request *r = by_left[k];
-        const int64_t s = left / (int64_t)(by_left.size() - k);
-        if (r->nphoton - r->issued > s) break;
-        r->slice = r->nphoton - r->issued;
-        left -= r->slice;
-      }
-      const int64_t s = k < by_left.size() ? std::max<int64_t>(1, left / (int64_t)(by_left.size() - k)) : 0;
-      for (; k < by_left.size(); k++) by_left[k]->slice = std::min(s, by_left[k]->nphoton - by_left[k]->issued);
+    // slices: shortest remaining first with a floor share (default), or water-filling
+    // (epoch_plan.hpp)
+    {
+      std::vector<int64_t> left;
+      for (Request *r : open) left.push_back(r->nphoton - r->issued);
+      const std::vector<int64_t> sl = epoch_slices(left, epoch, cfg.slicing != VMC_SLICE_EQUAL);
+      for (size_t i = 0; i < open.size(); i++) open[i]->slice = sl[i];
     }
     struct Cls { int dim; bool fd; std::vector<Request *> rs; };
     std::vector<Cls> classes;
