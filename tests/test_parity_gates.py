@@ -78,3 +78,20 @@ def test_integrated_gate_catches_a_uniform_absorption_offset(square, reference_s
     gpu, null = _gpu_side(square.copy(mua=square.mua * 1.05))
     _, scalars_ok = _verdicts("mua x 1.05", gpu, null, reference_side)
     assert not scalars_ok
+
+
+def test_bench_error_to_noise_reads_one_for_a_match_and_more_for_an_error(square, reference_side):
+    """bench.py's matched-error figure (error-to-noise: sqrt of chi2/dof against the oracle
+    over chi2/dof against independent batches of the oracle's size) on the same known
+    answers: near 1 for the exact match, well above the 1.1 target for the planted phase
+    function error."""
+    import bench
+    ref = [r.ER for r in reference_side]
+    gpu, null = _gpu_side(square)
+    exact = bench.welch_error_to_noise([r.ER for r in gpu], ref, [r.ER for r in null])
+    gpu_bad, null_bad = _gpu_side(square.copy(g=np.full_like(square.g, 0.89)))
+    bad = bench.welch_error_to_noise([r.ER for r in gpu_bad], ref, [r.ER for r in null_bad])
+    print("error-to-noise: exact", exact, "g 0.89", bad)
+    assert exact["elements"] >= 100 and bad["elements"] >= 100
+    assert 0.7 < exact["error_to_noise"] < 1.1
+    assert bad["error_to_noise"] > 1.5
